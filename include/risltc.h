@@ -1,0 +1,306 @@
+/* risltc.h - C ABI of the GB300 implementation of risltc's per-pixel shading
+ * path: RIS over polygonal lights with an LTC-integral target, projected
+ * solid angle sampling of the chosen polygon, shadow-ray visibility and the
+ * MIS combine.
+ *
+ * The first half repeats the reference's own host-side API verbatim (types,
+ * enums and functions of src/polygonal_light.h, src/ltc_table.h,
+ * src/noise_table.h and src/main.h), so C99 host code written against the
+ * reference compiles unchanged.  The second half replaces what the reference
+ * does through Vulkan (LTC texture upload, light buffer, acceleration
+ * structure, the full-screen shading draw) with plain functions over host or
+ * device pointers.
+ *
+ * Conventions: every function returns an int status (RISLTC_OK == 0) unless
+ * it mirrors a reference function with another signature; no function prints,
+ * aborts or traps.  A context is bound to one device and one CUDA stream and
+ * is not thread-safe; distinct contexts may be used concurrently.  All device
+ * work is stream-ordered.
+ */
+#ifndef RISLTC_H
+#define RISLTC_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define EXTERN_C extern "C"
+#else
+#define EXTERN_C
+#endif
+
+/* ======================================================================== */
+/* Reference API (verbatim)                                                 */
+/* ======================================================================== */
+
+/* src/polygonal_light.h:31-46 */
+typedef enum sample_polygon_technique_e {
+	sample_polygon_baseline,
+	sample_polygon_area_turk,
+	sample_polygon_projected_solid_angle,
+	sample_polygon_projected_solid_angle_biased,
+	sample_polygon_ltc_cp,
+	sample_polygon_count
+} sample_polygon_technique_t;
+
+/* src/polygonal_light.h:52-67 */
+typedef enum polygon_texturing_technique_e {
+	polygon_texturing_none = 0,
+	polygon_texturing_area = 1,
+	polygon_texturing_portal = 2,
+	polygon_texturing_ies_profile = 3,
+	polygon_texturing_count,
+	polygon_texturing_force_int = 0x7fffffff
+} polygon_texturing_technique_t;
+
+/* src/polygonal_light.h:73-99.  Host description of a convex polygonal
+   light: Euler angles, scalings, translation and plane-space vertices in;
+   world-space vertices, plane, area and radiance written by
+   update_polygonal_light(). */
+typedef struct polygonal_light_s {
+	float rotation_angles[3];
+	float scaling_x;
+	float translation[3];
+	float scaling_y;
+	float radiant_flux[3];
+	float inv_scaling_x;
+	float surface_radiance[3];
+	float inv_scaling_y;
+	float plane[4];
+	uint32_t vertex_count;
+	polygon_texturing_technique_t texturing_technique;
+	uint32_t texture_index;
+	uint32_t padding_0;
+	float rotation[3][4];
+	float area, rcp_area;
+	float padding_1[2];
+	char* texture_file_path;
+	float* vertices_plane_space;
+	float* vertices_world_space;
+} polygonal_light_t;
+
+/* src/polygonal_light.h:104-111: the fixed part of one light in the
+   shader's std140 light buffer. */
+typedef struct polygonal_light_upload_s {
+	float surface_radiance[3];
+	float padding_1;
+	float plane[4];
+	uint32_t vertex_count;
+	float padding_2[3];
+} polygonal_light_upload_t;
+
+/* src/polygonal_light.h:115-119 */
+#define POLYGONAL_LIGHT_QUICKSAVE_SIZE (sizeof(float) * 20 + sizeof(uint32_t) * 2)
+#define POLYGONAL_LIGHT_FIXED_CONSTANT_BUFFER_SIZE (sizeof(float) * 12)
+
+/* src/main.h:59-77 */
+typedef enum mis_heuristic_e {
+	mis_heuristic_balance,
+	mis_heuristic_power,
+	mis_heuristic_weighted,
+	mis_heuristic_optimal_clamped,
+	mis_heuristic_optimal,
+	mis_heuristic_count
+} mis_heuristic_t;
+
+/* src/main.h:79-84 */
+typedef enum light_sampling_strategies_e { light_uniform, light_reservoir } light_sampling_strategies_t;
+
+/* src/ltc_table.h:23-35 */
+typedef struct ltc_constants_s {
+	float fresnel_index_factor, fresnel_index_summand;
+	float roughness_factor, roughness_summand;
+	float inclination_factor, inclination_summand;
+	float padding[2];
+} ltc_constants_t;
+
+/* src/noise_table.h:25-29 */
+typedef struct noise_table_s {
+	uint32_t random_seed;
+} noise_table_t;
+
+/* src/polygonal_light.c:27-41.  Like the reference, the return value is
+   always 0 (it compares the count after assigning it). */
+EXTERN_C int set_polygonal_light_vertex_count(polygonal_light_t* light, uint32_t vertex_count);
+/* src/polygonal_light.c:44-98 */
+EXTERN_C void update_polygonal_light(polygonal_light_t* light);
+/* src/polygonal_light.c:101-110 */
+EXTERN_C polygonal_light_t duplicate_polygonal_light(const polygonal_light_t* light);
+/* src/polygonal_light.c:113-118 */
+EXTERN_C void destroy_polygonal_light(polygonal_light_t* light);
+/* src/noise_table.c:24-28 (VkBool32 animate_noise becomes uint32_t). */
+EXTERN_C void set_noise_constants(uint32_t resolution_mask[2], uint32_t* texture_index_mask, uint32_t random_numbers[4],
+                                  noise_table_t* noise, uint32_t animate_noise);
+
+/* ======================================================================== */
+/* GB300 replacement of the Vulkan-side path                                */
+/* ======================================================================== */
+
+enum risltc_status_e {
+	RISLTC_OK = 0,
+	RISLTC_ERROR_INVALID_ARGUMENT = 1,
+	RISLTC_ERROR_VERTEX_COUNT = 2,
+	RISLTC_ERROR_CUDA = 3,
+	RISLTC_ERROR_TRAVERSAL_LIMIT = 4,
+	RISLTC_ERROR_NON_FINITE = 5,
+	RISLTC_ERROR_NO_DEVICE = 6,
+	RISLTC_ERROR_OUT_OF_MEMORY = 7,
+	RISLTC_ERROR_IO = 8,
+	RISLTC_ERROR_UNSUPPORTED = 9
+};
+
+/* Largest light vertex count (MAX_POLYGONAL_LIGHT_VERTEX_COUNT of
+   main.c:181-204).  The reference's clipper covers 3..7 vertices; 8-vertex
+   lights are clipped by the same rule extended by one vertex. */
+#define RISLTC_MAX_LIGHT_VERTEX_COUNT 8
+
+/* wang_random_number, src/math_utilities.h:50-57 */
+EXTERN_C uint32_t risltc_wang_random_number(uint32_t seed);
+
+/* std140 light buffer exactly as write_lights (src/main.c:456-490) builds it
+   for the shader, except that every slot past vertex_count holds vertex 0
+   (the reference writes it to slot vertex_count only and leaves the rest
+   unwritten).  Calls update_polygonal_light() on each light.  data must hold
+   count * (12 + 4 * max_vertex_count) floats. */
+EXTERN_C int risltc_write_lights(float* data, polygonal_light_t* lights, uint32_t count, uint32_t max_vertex_count);
+/* get_max_polygonal_light_vertex_count, src/main.c:183-189 */
+EXTERN_C uint32_t risltc_max_light_vertex_count(const polygonal_light_t* lights, uint32_t count);
+
+/* LTC table in FP32 (the reference keeps two UNORM16 texture arrays,
+   src/ltc_table.h:41-57).  texels0: [fresnel][inclination][roughness][4] =
+   (m00, -m02, m11, m20) of the normalised inverse fit; texels1: [...][2] =
+   (m22, albedo). */
+typedef struct risltc_ltc_table_s {
+	uint32_t roughness_count, inclination_count, fresnel_count;
+	uint32_t padding;
+	float* texels0;
+	float* texels1;
+	ltc_constants_t constants;
+} risltc_ltc_table_t;
+
+/* The quantisation of load_ltc_table (src/ltc_table.c:82-116) and its
+   constants (:184-192) without Vulkan.  fit holds fresnel_count slices of
+   resolution^2 records of 5 floats (the records of fit<i>.dat after the
+   uint64 resolution header).  quantize_unorm16 != 0 rounds every stored value
+   to 16-bit UNORM as the reference's textures do. */
+EXTERN_C int risltc_ltc_table_from_fit(risltc_ltc_table_t* table, const float* fit, uint32_t resolution,
+                                       uint32_t fresnel_count, int quantize_unorm16);
+/* Reads directory/fit<i>.dat for i < fresnel_count (load_ltc_table's files). */
+EXTERN_C int risltc_load_ltc_table(risltc_ltc_table_t* table, const char* directory, uint32_t fresnel_count,
+                                   int quantize_unorm16);
+/* A smooth synthetic fit (positive diagonal, albedo in (0,1)) from a seed;
+   stands in for the reference's fit files, which are not distributed. */
+EXTERN_C int risltc_ltc_table_synthetic(risltc_ltc_table_t* table, uint64_t seed, uint32_t roughness_count,
+                                        uint32_t inclination_count);
+EXTERN_C void risltc_ltc_table_destroy(risltc_ltc_table_t* table);
+
+/* Binary BVH over triangles, built on the host by binned SAH.  Node =
+   8 x 32-bit words {bmin.xyz, left_or_first, bmax.xyz, count}; count == 0
+   marks an interior node with children left and left + 1; a leaf covers
+   triangles [first, first + count) of the reordered triangle array, 12 floats
+   each {v0, 0, v1 - v0, 0, v2 - v0, 0}.  Boxes are widened by a relative
+   1e-6 so that traversal never culls a box that holds a hit. */
+typedef struct risltc_bvh_s {
+	uint32_t node_count, triangle_count, depth;
+	uint32_t padding;
+	float* nodes;
+	float* triangles;
+	uint32_t* triangle_ids;
+} risltc_bvh_t;
+/* triangles: 9 floats per triangle (v0, v1, v2). */
+EXTERN_C int risltc_bvh_build(risltc_bvh_t* bvh, const float* triangles, uint32_t triangle_count, uint32_t max_leaf_size);
+EXTERN_C void risltc_bvh_destroy(risltc_bvh_t* bvh);
+
+/* Run settings: render_settings_t (src/main.h:123-156) reduced to what the
+   shading pass reads, plus the candidate count the reference hard-codes
+   (shading_pass.frag.glsl:726, 32). */
+typedef enum risltc_numerics_e {
+	/* IEEE division and square root, no contraction, the project's own
+	   transcendentals: bit-identical to the CPU oracle. */
+	risltc_numerics_exact = 0,
+	/* Hardware reciprocal square root, approximate division and
+	   contraction: faster, within the tolerance of the parity tests. */
+	risltc_numerics_fast = 1
+} risltc_numerics_t;
+
+typedef struct risltc_settings_s {
+	sample_polygon_technique_t polygon_sampling_technique; /* ltc_cp or projected_solid_angle(_biased) */
+	light_sampling_strategies_t light_sampling;
+	mis_heuristic_t mis_heuristic;
+	uint32_t candidate_count;   /* M */
+	uint32_t sample_count;      /* SAMPLE_COUNT */
+	uint32_t sample_count_light; /* LIGHT_SAMPLES */
+	float mis_visibility_estimate;
+	uint32_t fast_atan;
+	uint32_t shadows;           /* trace shadow rays through the scene BVH */
+	risltc_numerics_t numerics;
+} risltc_settings_t;
+
+/* specify_default_render_settings, src/main.c:220-236 (M = 32, shadows on) */
+EXTERN_C void risltc_default_settings(risltc_settings_t* settings);
+
+/* G-buffer: 17 planes of width*height floats in device memory (the fields
+   of shading_data_t, src/shaders/brdfs.glsl:22-39): position xyz, normal xyz,
+   outgoing xyz, lambert_outgoing, diffuse_albedo rgb, fresnel_0 rgb,
+   roughness.  primitive (optional) marks background with 0xFFFFFFFF. */
+#define RISLTC_GBUFFER_PLANES 17
+typedef struct risltc_gbuffer_s {
+	uint32_t width, height;
+	const float* planes;
+	const uint32_t* primitive;
+} risltc_gbuffer_t;
+
+/* The reservoir of reservoir.glsl:16-25 for the first light sample. */
+typedef struct risltc_reservoir_s {
+	int32_t light_index;
+	float w_sum;
+	float sample_value;
+	uint32_t padding;
+} risltc_reservoir_t;
+
+typedef struct risltc_ctx_s risltc_ctx_t;
+typedef struct risltc_scene_s risltc_scene_t;
+
+/* stream: a cudaStream_t, or NULL for the legacy default stream. */
+EXTERN_C int risltc_ctx_create(risltc_ctx_t** ctx, int device, void* stream);
+EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx);
+
+/* Uploads lights (the std140 buffer of risltc_write_lights), the LTC table
+   and, if triangle_count > 0, builds and uploads the BVH of the occluders
+   (9 floats per triangle).  All inputs are host memory. */
+EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, uint32_t light_count,
+                                 uint32_t max_vertex_count, const risltc_ltc_table_t* ltc, const float* triangles,
+                                 uint32_t triangle_count, risltc_scene_t** scene);
+EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene);
+
+/* Shades frame_count consecutive frames of the G-buffer (device pointers).
+ * Frame f uses the noise constants of set_noise_constants(..., noise,
+ * animate) called once per frame (noise->random_seed advances by
+ * frame_count).  out_rgb (device, width*height*3 floats, may be NULL) gets the
+ * mean over the frames; accum (device, width*height*3 doubles, may be NULL)
+ * gets the per-frame results added in FP64; reservoirs (device, may be NULL)
+ * gets the first frame's reservoir per pixel.  Stream-ordered; returns
+ * RISLTC_ERROR_TRAVERSAL_LIMIT etc. only through risltc_ctx_check(). */
+EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                          const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
+                          uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs);
+
+/* Same with host buffers: copies the G-buffer planes in, shades, copies
+ * out_rgb back, synchronises and reports device errors.  This is the call a
+ * host program makes per frame. */
+EXTERN_C int risltc_shade_host(risltc_ctx_t* ctx, const risltc_scene_t* scene, uint32_t width, uint32_t height,
+                               const float* gbuffer_planes, const uint32_t* primitive,
+                               const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
+                               uint32_t frame_count, float* out_rgb);
+
+/* Any-hit shadow queries through the scene BVH: rays are 8 floats
+   {origin xyz, t_min, direction xyz, t_max} in device memory; hits gets
+   1 (occluded) or 0 per ray. */
+EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene, const float* rays, uint32_t ray_count,
+                                 uint32_t* hits);
+
+/* Synchronises the context's stream and returns the first error recorded by
+   a kernel since the last check (RISLTC_OK if none). */
+EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx);
+EXTERN_C const char* risltc_status_string(int status);
+
+#endif /* RISLTC_H */

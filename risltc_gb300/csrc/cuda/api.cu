@@ -1,0 +1,328 @@
+// api.cu - the device half of the C ABI in include/risltc.h: contexts,
+// scene upload, frame shading and shadow queries.
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <cuda_runtime.h>
+#include "shade_kernel.cuh"
+
+namespace risltc {
+cudaError_t launch_shade_exact(const ShadeParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_shade_fast(const ShadeParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,
+                               cudaStream_t stream, int grid);
+}  // namespace risltc
+
+struct risltc_ctx_s {
+	int device;
+	cudaStream_t stream;
+	int sm_count;
+	uint32_t* d_error;
+	// Staging for risltc_shade_host, grown on demand.
+	float* d_gbuffer;
+	uint32_t* d_primitive;
+	float* d_rgb;
+	size_t pixel_capacity;
+	float* h_pinned_rgb;
+};
+
+struct risltc_scene_s {
+	risltc_ctx_t* ctx;
+	risltc::SceneView view;
+	void* d_lights;
+	void* d_ltc;
+	void* d_nodes;
+	void* d_triangles;
+	uint32_t max_vertex_count;
+	uint32_t bvh_depth;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+	if (e == cudaSuccess) return RISLTC_OK;
+	if (e == cudaErrorMemoryAllocation) return RISLTC_ERROR_OUT_OF_MEMORY;
+	if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return RISLTC_ERROR_NO_DEVICE;
+	return RISLTC_ERROR_CUDA;
+}
+
+int grid_for(const risltc_ctx_t* ctx, size_t items) {
+	// Resident CTAs per SM times SMs; the kernels are grid-stride loops.
+	size_t blocks = (items + 127) / 128;
+	size_t cap = (size_t) ctx->sm_count * 16;
+	if (blocks > cap) blocks = cap;
+	return (int) (blocks ? blocks : 1);
+}
+
+}  // namespace
+
+EXTERN_C int risltc_ctx_create(risltc_ctx_t** out, int device, void* stream) {
+	if (!out) return RISLTC_ERROR_INVALID_ARGUMENT;
+	*out = nullptr;
+	int count = 0;
+	cudaError_t e = cudaGetDeviceCount(&count);
+	if (e != cudaSuccess || count == 0) return RISLTC_ERROR_NO_DEVICE;
+	if (device < 0 || device >= count) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if ((e = cudaSetDevice(device)) != cudaSuccess) return cuda_status(e);
+	risltc_ctx_t* ctx = (risltc_ctx_t*) calloc(1, sizeof(risltc_ctx_t));
+	if (!ctx) return RISLTC_ERROR_OUT_OF_MEMORY;
+	ctx->device = device;
+	ctx->stream = (cudaStream_t) stream;
+	cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+	if ((e = cudaMalloc(&ctx->d_error, sizeof(uint32_t))) != cudaSuccess ||
+	    (e = cudaMemsetAsync(ctx->d_error, 0, sizeof(uint32_t), ctx->stream)) != cudaSuccess) {
+		cudaFree(ctx->d_error);
+		free(ctx);
+		return cuda_status(e);
+	}
+	*out = ctx;
+	return RISLTC_OK;
+}
+
+EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
+	if (!ctx) return;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_error);
+	cudaFree(ctx->d_gbuffer);
+	cudaFree(ctx->d_primitive);
+	cudaFree(ctx->d_rgb);
+	cudaFreeHost(ctx->h_pinned_rgb);
+	free(ctx);
+}
+
+EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, uint32_t light_count,
+                                 uint32_t max_vertex_count, const risltc_ltc_table_t* ltc, const float* triangles,
+                                 uint32_t triangle_count, risltc_scene_t** out) {
+	if (!ctx || !out || !lights_std140 || light_count == 0 || !ltc || !ltc->texels0 || !ltc->texels1 ||
+	    max_vertex_count < 3 || max_vertex_count > RISLTC_MAX_LIGHT_VERTEX_COUNT || (triangle_count && !triangles))
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	*out = nullptr;
+	cudaSetDevice(ctx->device);
+	// Lights: 128-byte records {radiance, vertex_count | plane | 8 vertices xyz}.
+	const size_t stride = 12 + 4 * (size_t) max_vertex_count;
+	std::vector<float> lights((size_t) light_count * risltc::kLightWords, 0.0f);
+	for (uint32_t i = 0; i != light_count; ++i) {
+		const float* s = lights_std140 + i * stride;
+		float* d = lights.data() + (size_t) i * risltc::kLightWords;
+		uint32_t vc;
+		memcpy(&vc, s + 8, 4);
+		if (vc < 3 || vc > max_vertex_count) return RISLTC_ERROR_VERTEX_COUNT;
+		d[0] = s[0];
+		d[1] = s[1];
+		d[2] = s[2];
+		memcpy(d + 3, &vc, 4);
+		for (int c = 0; c != 4; ++c) d[4 + c] = s[4 + c];
+		for (uint32_t v = 0; v != RISLTC_MAX_LIGHT_VERTEX_COUNT; ++v) {
+			const float* src = s + 12 + 4 * (v < vc ? v : 0);
+			d[8 + 3 * v + 0] = src[0];
+			d[8 + 3 * v + 1] = src[1];
+			d[8 + 3 * v + 2] = src[2];
+		}
+	}
+	// LTC: 8 floats per texel {m00, -m02, m11, m20, m22, albedo, 0, 0}.
+	size_t texels = (size_t) ltc->roughness_count * ltc->inclination_count * ltc->fresnel_count;
+	std::vector<float> ltc_dev(texels * risltc::kLtcTexelWords, 0.0f);
+	for (size_t t = 0; t != texels; ++t) {
+		for (int c = 0; c != 4; ++c) ltc_dev[8 * t + c] = ltc->texels0[4 * t + c];
+		ltc_dev[8 * t + 4] = ltc->texels1[2 * t + 0];
+		ltc_dev[8 * t + 5] = ltc->texels1[2 * t + 1];
+	}
+	risltc_bvh_t bvh;
+	memset(&bvh, 0, sizeof(bvh));
+	if (triangle_count) {
+		int st = risltc_bvh_build(&bvh, triangles, triangle_count, 4);
+		if (st) return st;
+	}
+	risltc_scene_t* scene = (risltc_scene_t*) calloc(1, sizeof(risltc_scene_t));
+	if (!scene) {
+		risltc_bvh_destroy(&bvh);
+		return RISLTC_ERROR_OUT_OF_MEMORY;
+	}
+	scene->ctx = ctx;
+	scene->max_vertex_count = max_vertex_count;
+	scene->bvh_depth = bvh.depth;
+	cudaError_t e = cudaSuccess;
+	auto upload = [&](void** dst, const void* src, size_t bytes) {
+		if (e != cudaSuccess || bytes == 0) return;
+		e = cudaMalloc(dst, bytes);
+		if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+	};
+	upload(&scene->d_lights, lights.data(), lights.size() * sizeof(float));
+	upload(&scene->d_ltc, ltc_dev.data(), ltc_dev.size() * sizeof(float));
+	if (triangle_count) {
+		upload(&scene->d_nodes, bvh.nodes, (size_t) bvh.node_count * 8 * sizeof(float));
+		upload(&scene->d_triangles, bvh.triangles, (size_t) bvh.triangle_count * 12 * sizeof(float));
+	}
+	risltc_bvh_destroy(&bvh);
+	if (e != cudaSuccess) {
+		risltc_scene_destroy(scene);
+		return cuda_status(e);
+	}
+	risltc::SceneView& v = scene->view;
+	v.lights = (const float4*) scene->d_lights;
+	v.light_count = (int) light_count;
+	v.ltc = (const float4*) scene->d_ltc;
+	v.ltc_width = (int) ltc->roughness_count;
+	v.ltc_height = (int) ltc->inclination_count;
+	v.ltc_layers = (int) ltc->fresnel_count;
+	v.ltc_constants[0] = ltc->constants.fresnel_index_factor;
+	v.ltc_constants[1] = ltc->constants.fresnel_index_summand;
+	v.ltc_constants[2] = ltc->constants.roughness_factor;
+	v.ltc_constants[3] = ltc->constants.roughness_summand;
+	v.ltc_constants[4] = ltc->constants.inclination_factor;
+	v.ltc_constants[5] = ltc->constants.inclination_summand;
+	v.nodes = (const float4*) scene->d_nodes;
+	v.triangles = (const float4*) scene->d_triangles;
+	v.triangle_count = (int) triangle_count;
+	*out = scene;
+	return RISLTC_OK;
+}
+
+EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene) {
+	if (!scene) return;
+	cudaSetDevice(scene->ctx->device);
+	cudaStreamSynchronize(scene->ctx->stream);
+	cudaFree(scene->d_lights);
+	cudaFree(scene->d_ltc);
+	cudaFree(scene->d_nodes);
+	cudaFree(scene->d_triangles);
+	free(scene);
+}
+
+static int validate_settings(const risltc_settings_t* s) {
+	if (!s) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (s->polygon_sampling_technique != sample_polygon_ltc_cp &&
+	    s->polygon_sampling_technique != sample_polygon_projected_solid_angle &&
+	    s->polygon_sampling_technique != sample_polygon_projected_solid_angle_biased)
+		return RISLTC_ERROR_UNSUPPORTED;
+	if ((int) s->mis_heuristic < 0 || s->mis_heuristic >= mis_heuristic_count) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (s->light_sampling != light_uniform && s->light_sampling != light_reservoir) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (s->candidate_count < 1 || s->candidate_count > 4096 || s->sample_count < 1 || s->sample_count > 64 ||
+	    s->sample_count_light < 1 || s->sample_count_light > 64)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (s->numerics != risltc_numerics_exact && s->numerics != risltc_numerics_fast) return RISLTC_ERROR_INVALID_ARGUMENT;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                          const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
+                          uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs) {
+	if (!ctx || !scene || !gbuffer || !gbuffer->planes || !noise || frame_count == 0 || gbuffer->width == 0 ||
+	    gbuffer->height == 0 || (uint64_t) gbuffer->width * gbuffer->height > 0xffffffffull / 32)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	int st = validate_settings(settings);
+	if (st) return st;
+	risltc::ShadeParams p;
+	memset(&p, 0, sizeof(p));
+	p.scene = scene->view;
+	p.gbuffer = gbuffer->planes;
+	p.primitive = gbuffer->primitive;
+	p.width = gbuffer->width;
+	p.height = gbuffer->height;
+	p.technique = (int) settings->polygon_sampling_technique;
+	p.light_sampling = (int) settings->light_sampling;
+	p.mis_heuristic = (int) settings->mis_heuristic;
+	p.candidate_count = (int) settings->candidate_count;
+	p.sample_count = (int) settings->sample_count;
+	p.light_samples = (int) settings->sample_count_light;
+	p.mis_visibility_estimate = settings->mis_visibility_estimate;
+	p.fast_atan = (int) settings->fast_atan;
+	p.shadows = (int) settings->shadows;
+	p.noise_seed = noise->random_seed;
+	p.animate = animate;
+	p.frame_count = frame_count;
+	p.out_rgb = out_rgb;
+	p.accum = accum;
+	p.reservoirs = reservoirs;
+	p.error = ctx->d_error;
+	cudaSetDevice(ctx->device);
+	int grid = grid_for(ctx, (size_t) gbuffer->width * gbuffer->height);
+	cudaError_t e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_shade_fast(p, ctx->stream, grid)
+	                                                             : risltc::launch_shade_exact(p, ctx->stream, grid);
+	if (e != cudaSuccess) return cuda_status(e);
+	noise->random_seed += frame_count;
+	return RISLTC_OK;
+}
+
+static int ensure_staging(risltc_ctx_t* ctx, size_t pixels) {
+	if (pixels <= ctx->pixel_capacity) return RISLTC_OK;
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_gbuffer);
+	cudaFree(ctx->d_primitive);
+	cudaFree(ctx->d_rgb);
+	ctx->d_gbuffer = nullptr;
+	ctx->d_primitive = nullptr;
+	ctx->d_rgb = nullptr;
+	ctx->pixel_capacity = 0;
+	cudaError_t e = cudaMalloc(&ctx->d_gbuffer, pixels * RISLTC_GBUFFER_PLANES * sizeof(float));
+	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_primitive, pixels * sizeof(uint32_t));
+	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rgb, pixels * 3 * sizeof(float));
+	if (e != cudaSuccess) return cuda_status(e);
+	ctx->pixel_capacity = pixels;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_shade_host(risltc_ctx_t* ctx, const risltc_scene_t* scene, uint32_t width, uint32_t height,
+                               const float* gbuffer_planes, const uint32_t* primitive,
+                               const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
+                               uint32_t frame_count, float* out_rgb) {
+	if (!ctx || !scene || !gbuffer_planes || !out_rgb || width == 0 || height == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(ctx->device);
+	size_t pixels = (size_t) width * height;
+	int st = ensure_staging(ctx, pixels);
+	if (st) return st;
+	cudaError_t e = cudaMemcpyAsync(ctx->d_gbuffer, gbuffer_planes, pixels * RISLTC_GBUFFER_PLANES * sizeof(float),
+	                                cudaMemcpyHostToDevice, ctx->stream);
+	if (e == cudaSuccess && primitive)
+		e = cudaMemcpyAsync(ctx->d_primitive, primitive, pixels * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+	if (e != cudaSuccess) return cuda_status(e);
+	risltc_gbuffer_t g = {width, height, ctx->d_gbuffer, primitive ? ctx->d_primitive : nullptr};
+	st = risltc_shade(ctx, scene, &g, settings, noise, animate, frame_count, ctx->d_rgb, nullptr, nullptr);
+	if (st) return st;
+	e = cudaMemcpyAsync(out_rgb, ctx->d_rgb, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+	if (e != cudaSuccess) return cuda_status(e);
+	return risltc_ctx_check(ctx);
+}
+
+EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene, const float* rays, uint32_t ray_count,
+                                 uint32_t* hits) {
+	if (!ctx || !scene || (ray_count && (!rays || !hits))) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (ray_count == 0) return RISLTC_OK;
+	cudaSetDevice(ctx->device);
+	cudaError_t e = risltc::launch_trace_exact(scene->view, (const float4*) rays, ray_count, hits, ctx->d_error,
+	                                           ctx->stream, grid_for(ctx, ray_count));
+	return cuda_status(e);
+}
+
+EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx) {
+	if (!ctx) return RISLTC_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(ctx->device);
+	uint32_t bits = 0;
+	cudaError_t e = cudaMemcpyAsync(&bits, ctx->d_error, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+	if (e != cudaSuccess) return cuda_status(e);
+	if (bits) {
+		cudaMemsetAsync(ctx->d_error, 0, sizeof(uint32_t), ctx->stream);
+		cudaStreamSynchronize(ctx->stream);
+		if (bits & risltc::kErrorTraversalLimit) return RISLTC_ERROR_TRAVERSAL_LIMIT;
+		return RISLTC_ERROR_VERTEX_COUNT;
+	}
+	return RISLTC_OK;
+}
+
+EXTERN_C const char* risltc_status_string(int status) {
+	switch (status) {
+	case RISLTC_OK: return "ok";
+	case RISLTC_ERROR_INVALID_ARGUMENT: return "invalid argument";
+	case RISLTC_ERROR_VERTEX_COUNT: return "light vertex count outside 3..8 (or above the scene maximum)";
+	case RISLTC_ERROR_CUDA: return "CUDA error";
+	case RISLTC_ERROR_TRAVERSAL_LIMIT: return "BVH traversal exceeded its iteration or stack limit";
+	case RISLTC_ERROR_NON_FINITE: return "non-finite input";
+	case RISLTC_ERROR_NO_DEVICE: return "no CUDA device";
+	case RISLTC_ERROR_OUT_OF_MEMORY: return "out of memory";
+	case RISLTC_ERROR_IO: return "file could not be read";
+	case RISLTC_ERROR_UNSUPPORTED: return "unsupported setting";
+	default: return "unknown status";
+	}
+}

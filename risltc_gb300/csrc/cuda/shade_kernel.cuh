@@ -1,0 +1,355 @@
+// shade_kernel.cuh - the per-pixel shading kernel and the shadow-ray kernel.
+// Instantiated by shade_exact.cu and shade_fast.cu with one numerics policy.
+#pragma once
+#include "shade_psa.cuh"
+
+namespace risltc {
+
+enum : uint32_t {
+	kErrorTraversalLimit = 1u << 0,
+	kErrorVertexCount = 1u << 1,
+};
+
+struct ShadeParams {
+	SceneView scene;
+	const float* gbuffer;        // 17 planes
+	const uint32_t* primitive;   // may be null
+	uint32_t width, height;
+	int technique;               // sample_polygon_technique_t
+	int light_sampling;          // light_sampling_strategies_t
+	int mis_heuristic;
+	int candidate_count;
+	int sample_count;
+	int light_samples;
+	float mis_visibility_estimate;
+	int fast_atan;
+	int shadows;
+	uint32_t noise_seed;         // noise_table_t::random_seed of the first frame
+	uint32_t animate;
+	uint32_t frame_count;
+	float* out_rgb;              // may be null
+	double* accum;               // may be null
+	risltc_reservoir_t* reservoirs;  // may be null
+	uint32_t* error;             // error bits (atomicOr)
+};
+
+// Any-hit query against the BVH (stack traversal, near child first is not
+// needed for any-hit).  Returns true if occluded.  Gives up after
+// kTraversalLimit node visits, records the error and reports "not occluded".
+template <class P> RL_DEV bool any_hit(const SceneView& s, f3 o, f3 d, float t_min, float t_max, uint32_t* error) {
+	if (s.triangle_count == 0) return false;
+	float inv[3] = {P::rcp(d.x), P::rcp(d.y), P::rcp(d.z)};
+	float org[3] = {o.x, o.y, o.z};
+	int32_t stack[kBvhStack];
+	int sp = 0;
+	stack[sp++] = 0;
+	uint32_t visits = 0;
+	while (sp > 0) {
+		if (++visits > kTraversalLimit) {
+			atomicOr(error, kErrorTraversalLimit);
+			return false;
+		}
+		int32_t ni = stack[--sp];
+		float4 a = __ldg(s.nodes + 2 * (size_t) ni), b = __ldg(s.nodes + 2 * (size_t) ni + 1);
+		float lo = t_min, hi = t_max;
+		float bmin[3] = {a.x, a.y, a.z}, bmax[3] = {b.x, b.y, b.z};
+#pragma unroll
+		for (int ax = 0; ax != 3; ++ax) {
+			float t0 = (bmin[ax] - org[ax]) * inv[ax];
+			float t1 = (bmax[ax] - org[ax]) * inv[ax];
+			float tn = t0 < t1 ? t0 : t1, tf = t0 < t1 ? t1 : t0;
+			if (tn == tn && tn > lo) lo = tn;
+			if (tf == tf && tf < hi) hi = tf;
+		}
+		if (!(lo <= hi)) continue;
+		int32_t first = __float_as_int(a.w), count = __float_as_int(b.w);
+		if (count == 0) {
+			if (sp + 2 > kBvhStack) {
+				atomicOr(error, kErrorTraversalLimit);
+				return false;
+			}
+			stack[sp++] = first + 1;
+			stack[sp++] = first;
+		} else {
+			for (int k = 0; k != count; ++k) {
+				const float4* t = s.triangles + 3 * (size_t) (first + k);
+				float4 q0 = __ldg(t), q1 = __ldg(t + 1), q2 = __ldg(t + 2);
+				f3 v0 = mk3(q0.x, q0.y, q0.z), e1 = mk3(q1.x, q1.y, q1.z), e2 = mk3(q2.x, q2.y, q2.z);
+				f3 p = cross(d, e2);
+				float det = dot(e1, p);
+				if (!(det != 0.0f)) continue;
+				float id = P::rcp(det);
+				f3 sv = sub(o, v0);
+				float u = dot(sv, p) * id;
+				if (!(u >= 0.0f && u <= 1.0f)) continue;
+				f3 q = cross(sv, e1);
+				float v = dot(d, q) * id;
+				if (!(v >= 0.0f && u + v <= 1.0f)) continue;
+				float tt = dot(e2, q) * id;
+				if (tt >= t_min && tt <= t_max) return true;
+			}
+		}
+	}
+	return false;
+}
+
+// get_polygon_visibility, shading_pass.frag.glsl:112-129
+template <class P>
+RL_DEV bool polygon_visibility(const ShadeParams& pr, bool visibility, f3 dir, f3 p, const Light& l) {
+	if (!visibility) return false;
+	if (!pr.shadows || pr.scene.triangle_count == 0) return true;
+	float max_t = P::div(-plane_dot(p, l.plane), dir.x * l.plane[0] + dir.y * l.plane[1] + dir.z * l.plane[2]);
+	max_t -= 1e-3f;
+	return !any_hit<P>(pr.scene, p, dir, 1.0e-3f, max_t, pr.error);
+}
+
+RL_DEV void side_flip(Ltc& ltc, const ShadingData& sd, const Light& l) {
+	float side = plane_dot(sd.position, l.plane);
+#pragma unroll
+	for (int i = 0; i != 4; ++i) ltc.world_to_shading.c[i].y = (side < 0.0f) ? -ltc.world_to_shading.c[i].y : ltc.world_to_shading.c[i].y;
+}
+
+// RIS target of the LTC_CP technique, shading_pass.frag.glsl:421-456
+template <class P> RL_DEV f3 ltc_cp_target(const ShadingData& sd, Ltc ltc, const Light& l) {
+	side_flip(ltc, sd, l);
+	uint32_t n = l.vertex_count;
+	f3 verts[kMaxPolygonVertices];
+#pragma unroll
+	for (int i = 0; i != kMaxLightVertices; ++i)
+		if (i < (int) n) verts[i] = mul_point(ltc.world_to_shading, l.v[i]);
+	uint32_t vc = clip_polygon<P>(n, verts);
+	f3 result = splat(0.0f);
+	f3 diffuse = splat(0.0f);
+	if (vc > 0) diffuse = mul(scale(sd.diffuse_albedo, calculate_ltc<P>(vc, verts)), l.radiance);
+	result = add(result, diffuse);
+	mat43 w2c = mul(ltc.shading_to_cosine, ltc.world_to_shading);
+#pragma unroll
+	for (int i = 0; i != kMaxLightVertices; ++i)
+		if (i < (int) n) verts[i] = mul_point(w2c, l.v[i]);
+	vc = clip_polygon<P>(n, verts);
+	f3 ggx = splat(0.0f);
+	if (vc > 0) ggx = mul(splat(calculate_ltc<P>(vc, verts) * ltc.albedo), l.radiance);
+	return add(result, ggx);
+}
+
+// evaluate_polygonal_light_shading_peters (peters = true,
+// shading_pass.frag.glsl:292-397) and the PSA branch of
+// evaluate_polygonal_light_shading (peters = false, :458-550)
+template <class P>
+RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l, uint32_t& seed,
+                        bool peters, bool visibility_in) {
+	const bool fa = pr.fast_atan != 0;
+	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
+	f3 result = splat(0.0f);
+	side_flip(ltc, sd, l);
+	PsaPolygon pd, ps;
+	uint32_t n = l.vertex_count;
+	for (int i = 0; i != 2; ++i) {
+		mat43 w2l = (i == 0) ? ltc.world_to_shading : mul(ltc.shading_to_cosine, ltc.world_to_shading);
+		f3 verts[kMaxPolygonVertices];
+#pragma unroll
+		for (int j = 0; j != kMaxLightVertices; ++j)
+			if (j < (int) n) verts[j] = mul_point(w2l, l.v[j]);
+		uint32_t vc = clip_polygon<P>(n, verts);
+		if (vc == 0 && i == 0) return result;
+		if (vc == 0) {
+			ps.psa = 0.0f;
+			break;
+		}
+		if (i == 0)
+			prepare_psa<P>(pd, vc, verts, fa);
+		else
+			prepare_psa<P>(ps, vc, verts, fa);
+	}
+	if (pd.psa == 0.0f) return result;
+	float specular_weight = ltc.albedo * ps.psa;
+	f3 diffuse_weight = scale(max3(sd.diffuse_albedo, splat(0.01f)), pd.psa);
+	int technique_count = (ps.psa > 0.0f) ? 2 : 1;
+	float rcp_d = P::rcp(pd.psa);
+	float rcp_s = P::rcp(ps.psa);
+	f3 specular_weight_rgb = splat(specular_weight);
+	if (pr.mis_heuristic == mis_heuristic_optimal) {
+		f3 rop = scale(l.radiance, kInvPi);
+		diffuse_weight = mul(diffuse_weight, rop);
+		specular_weight_rgb = mul(specular_weight_rgb, rop);
+	}
+	for (int i = 0; i != pr.sample_count; ++i) {
+		f3 dir_d = sample_psa<P>(pd, get_noise_2(seed), fa, biased);
+		f3 dir_s = mk3(0.0f, 0.0f, 1.0f);
+		if (ps.psa > 0.0f) {
+			dir_s = sample_psa<P>(ps, get_noise_2(seed), fa, biased);
+			dir_s = normalize<P>(mul(ltc.cosine_to_shading, dir_s));
+		}
+		for (int j = 0; j != technique_count; ++j) {
+			f3 dir = (j == 0) ? dir_d : dir_s;
+			if (dir.z <= 0.0f) continue;
+			float diffuse_density = dir.z * rcp_d;
+			float specular_density = evaluate_ltc_density<P>(ltc, dir, rcp_s);
+			f3 world_dir = transpose_mul(ltc.world_to_shading, dir);
+			f3 integrand;
+			bool visibility;
+			if (peters) {
+				visibility = dot(sd.normal, world_dir) > 0.0f;
+				visibility = polygon_visibility<P>(pr, visibility, world_dir, sd.position, l);
+				f3 rb = visibility ? mul(l.radiance, evaluate_brdf<P>(sd, world_dir)) : splat(0.0f);
+				integrand = scale(rb, dir.z);
+			} else {
+				bool cur = visibility_in;
+				bool side_vis = dot(sd.normal, world_dir) > 0.0f;
+				f3 rb;
+				if (!side_vis) {
+					rb = splat(0.0f);
+				} else {
+					cur = polygon_visibility<P>(pr, cur, world_dir, sd.position, l);
+					cur = side_vis && cur;
+					rb = mul(l.radiance, evaluate_brdf<P>(sd, world_dir));
+				}
+				integrand = scale(rb, dir.z);
+				integrand = (cur || !visibility_in) ? integrand : splat(0.0f);
+				visibility = true;
+			}
+			if (j == 0 && ps.psa <= 0.0f)
+				result = add(result, visibility ? scale(integrand, P::rcp(diffuse_density)) : splat(0.0f));
+			else if (j == 0)
+				result = add(result, mis_estimate<P>(pr.mis_heuristic, integrand, diffuse_weight, diffuse_density,
+				                                     specular_weight_rgb, specular_density, pr.mis_visibility_estimate));
+			else
+				result = add(result, mis_estimate<P>(pr.mis_heuristic, integrand, specular_weight_rgb, specular_density,
+				                                     diffuse_weight, diffuse_density, pr.mis_visibility_estimate));
+		}
+	}
+	return scale(result, P::rcp((float) pr.sample_count));
+}
+
+// Body of shading_pass.frag.glsl:main (:674-770) for one pixel and frame.
+template <class P>
+RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& ltc, uint32_t seed, bool first_frame,
+                      risltc_reservoir_t* res_out) {
+	const int n = pr.scene.light_count;
+	const bool peters = pr.technique == sample_polygon_ltc_cp;
+	f3 final_color = splat(0.0f);
+	risltc_reservoir_t rec;
+	rec.light_index = -1;
+	rec.w_sum = 0.0f;
+	rec.sample_value = 0.0f;
+	rec.padding = 0;
+	if (pr.light_sampling == light_uniform) {
+		for (int i = 0; i != pr.light_samples; ++i) {
+			int idx = (int) (get_noise_1(seed) * (float) n);
+			idx = idx > n - 1 ? n - 1 : idx;
+			Light l;
+			load_light(pr.scene, idx, l);
+			f3 r = scale(psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true), (float) n);
+			float ls = (float) pr.light_samples;
+			r = mk3(P::div(r.x, ls), P::div(r.y, ls), P::div(r.z, ls));
+			final_color = add(final_color, scale(r, 1.0f));
+			if (i == 0) rec.light_index = idx;
+		}
+	} else {
+		for (int j = 0; j != pr.light_samples; ++j) {
+			float w_sum = 0.0f, sample_value = 0.0f;
+			int res_index = -1;
+			const int m = pr.candidate_count;
+			const float p = P::rcp((float) n);
+			for (int i = 0; i != m; ++i) {
+				int idx = (int) (get_noise_1(seed) * (float) n);
+				idx = idx > n - 1 ? n - 1 : idx;
+				Light l;
+				load_light(pr.scene, idx, l);
+				f3 color = peters ? ltc_cp_target<P>(sd, ltc, l) : psa_mis_shade<P>(pr, sd, ltc, l, seed, false, false);
+				float p_hat = P::sqrt(dot(color, color));
+				float w = P::div(p_hat, p);
+				// insert_in_reservoir, reservoir.glsl:34-41
+				float rnd = get_noise_1(seed);
+				w_sum += w;
+				if (w > 0.0f && rnd < P::div(w, w_sum)) {
+					res_index = idx;
+					sample_value = p_hat;
+				}
+			}
+			if (j == 0) {
+				rec.light_index = res_index;
+				rec.w_sum = w_sum;
+				rec.sample_value = sample_value;
+			}
+			if (res_index >= 0) {
+				Light l;
+				load_light(pr.scene, res_index, l);
+				f3 color = psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true);
+				float W = P::div(w_sum, (float) m * sample_value);
+				if (sample_value == 0.0f) W = 0.0f;
+				f3 cw = scale(color, W);
+				float ls = (float) pr.light_samples;
+				final_color = add(final_color, mk3(P::div(cw.x, ls), P::div(cw.y, ls), P::div(cw.z, ls)));
+			}
+		}
+	}
+	if (isnan(final_color.x) || isnan(final_color.y) || isnan(final_color.z) || isinf(final_color.x) ||
+	    isinf(final_color.y) || isinf(final_color.z))
+		final_color = mk3(1.0f, 0.0f, 0.8f);
+	if (first_frame && res_out) *res_out = rec;
+	return final_color;
+}
+
+template <class P> __global__ void __launch_bounds__(128) shade_kernel(ShadeParams pr) {
+	const uint32_t np = pr.width * pr.height;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+		const uint32_t x = i % pr.width, y = i / pr.width;
+		risltc_reservoir_t* res = pr.reservoirs ? pr.reservoirs + i : nullptr;
+		if (pr.primitive && pr.primitive[i] == 0xffffffffu) {
+			if (res) *res = risltc_reservoir_t{-1, 0.0f, 0.0f, 0u};
+			if (pr.out_rgb) {
+				pr.out_rgb[3 * (size_t) i + 0] = 0.0f;
+				pr.out_rgb[3 * (size_t) i + 1] = 0.0f;
+				pr.out_rgb[3 * (size_t) i + 2] = 0.0f;
+			}
+			continue;
+		}
+		const float* g = pr.gbuffer;
+		ShadingData sd;
+		sd.position = mk3(g[0 * (size_t) np + i], g[1 * (size_t) np + i], g[2 * (size_t) np + i]);
+		sd.normal = mk3(g[3 * (size_t) np + i], g[4 * (size_t) np + i], g[5 * (size_t) np + i]);
+		sd.outgoing = mk3(g[6 * (size_t) np + i], g[7 * (size_t) np + i], g[8 * (size_t) np + i]);
+		sd.lambert_outgoing = g[9 * (size_t) np + i];
+		sd.diffuse_albedo = mk3(g[10 * (size_t) np + i], g[11 * (size_t) np + i], g[12 * (size_t) np + i]);
+		sd.fresnel_0 = mk3(g[13 * (size_t) np + i], g[14 * (size_t) np + i], g[15 * (size_t) np + i]);
+		sd.roughness = g[16 * (size_t) np + i];
+		float fl = dot(sd.fresnel_0, mk3(0.2126f, 0.7152f, 0.0722f));
+		const Ltc ltc = get_ltc_coefficients<P>(pr.scene, fl, sd.roughness, sd.position, sd.normal, sd.outgoing);
+		f3 sum = splat(0.0f);
+		double acc[3] = {0.0, 0.0, 0.0};
+		for (uint32_t f = 0; f != pr.frame_count; ++f) {
+			uint32_t rn_x = pr.animate ? wang_random_number((pr.noise_seed + f) * 4u) : 0u;
+			uint32_t seed = get_noise_accessor(x, y, pr.width, rn_x);
+			f3 c = shade_pixel<P>(pr, sd, ltc, seed, f == 0, res);
+			sum = add(sum, c);
+			acc[0] += (double) c.x;
+			acc[1] += (double) c.y;
+			acc[2] += (double) c.z;
+		}
+		if (pr.out_rgb) {
+			float inv = 1.0f / (float) pr.frame_count;
+			f3 mean = pr.frame_count == 1 ? sum : scale(sum, inv);
+			pr.out_rgb[3 * (size_t) i + 0] = mean.x;
+			pr.out_rgb[3 * (size_t) i + 1] = mean.y;
+			pr.out_rgb[3 * (size_t) i + 2] = mean.z;
+		}
+		if (pr.accum) {
+			pr.accum[3 * (size_t) i + 0] += acc[0];
+			pr.accum[3 * (size_t) i + 1] += acc[1];
+			pr.accum[3 * (size_t) i + 2] += acc[2];
+		}
+	}
+}
+
+// Batch of independent any-hit queries (risltc_trace_shadow).
+template <class P>
+__global__ void __launch_bounds__(128) trace_shadow_kernel(SceneView s, const float4* rays, uint32_t count,
+                                                          uint32_t* hits, uint32_t* error) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+		float4 a = rays[2 * (size_t) i], b = rays[2 * (size_t) i + 1];
+		hits[i] = any_hit<P>(s, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), a.w, b.w, error) ? 1u : 0u;
+	}
+}
+
+}  // namespace risltc
