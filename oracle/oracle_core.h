@@ -502,6 +502,12 @@ static void sort_convex_polygon_vertices(projected_solid_angle_polygon_t* p) {
 		compare_and_swap(p, 4, 5);
 		compare_and_swap(p, 1, 3);
 		break;
+	case 9:
+		/* Only 8-gons clipped to 9 vertices get here (the reference stops at
+		   8-vertex networks): adjacent compare-and-swap passes. */
+		for (uint32_t i = 1; i != 9; ++i)
+			for (uint32_t j = i; j != 0; --j) compare_and_swap(p, j - 1, j);
+		break;
 	default:
 		break;
 	}

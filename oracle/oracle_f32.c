@@ -19,3 +19,78 @@
 #define ORACLE_SUFFIX _f32
 #define ORACLE_OUT_T float
 #include "oracle_core.h"
+
+/* Internal routines exported for known-answer tests. */
+uint32_t oracle_f32_clip_polygon(uint32_t n, float* xyz, uint32_t max_polygon_vertex_count, int reference_limits) {
+	vec3_t v[OR_MAXP];
+	for (uint32_t i = 0; i != max_polygon_vertex_count; ++i) v[i] = V3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+	uint32_t vc = clip_polygon(n, v, max_polygon_vertex_count, reference_limits);
+	for (uint32_t i = 0; i != max_polygon_vertex_count; ++i) {
+		xyz[3 * i] = v[i].x;
+		xyz[3 * i + 1] = v[i].y;
+		xyz[3 * i + 2] = v[i].z;
+	}
+	return vc;
+}
+float oracle_f32_calculate_ltc(uint32_t vc, const float* xyz) {
+	vec3_t v[OR_MAXP];
+	for (uint32_t i = 0; i != vc; ++i) v[i] = V3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+	return calculate_ltc(vc, v, vc, 0);
+}
+/* Prepares PSA sampling of a clipped polygon (first vertex not repeated) and
+   draws count samples from the given random pairs; returns the polygon's
+   projected solid angle. */
+float oracle_f32_psa_sample(uint32_t vc, const float* xyz, uint32_t count, const float* rnd, float* out_dirs,
+                            float* out_errors) {
+	vec3_t v[OR_MAXP + 1];
+	for (uint32_t i = 0; i != vc; ++i) v[i] = V3(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+	v[vc] = v[0];
+	projected_solid_angle_polygon_t p;
+	g_oracle_fast_atan = 0;
+	g_oracle_biased_psa = 0;
+	prepare_projected_solid_angle_polygon_sampling(&p, vc, v, vc + 1);
+	for (uint32_t k = 0; k != count; ++k) {
+		vec3_t d = sample_projected_solid_angle_polygon(&p, V2(rnd[2 * k], rnd[2 * k + 1]), vc + 1);
+		out_dirs[3 * k] = d.x;
+		out_dirs[3 * k + 1] = d.y;
+		out_dirs[3 * k + 2] = d.z;
+		if (out_errors) {
+			/* Backward error: area from the sector start to the sample versus
+			   the target (compute_projected_solid_angle_polygon_sampling_error,
+			   polygon_sampling.glsl:846-906, first component). */
+			out_errors[k] = 0.0f;
+			if (!is_central_case(&p)) {
+				float target = rnd[2 * k] * p.projected_solid_angle;
+				float sector = 0.0f;
+				vec2_t outer = V2(0.0f, 0.0f), inner = p.inner_ellipse_0, dir_0 = V2(0.0f, 0.0f);
+				for (uint32_t i = 0; i != vc; ++i) {
+					if ((i > 1 && i + 1 == vc) || (i > 0 && target < 0.0f)) break;
+					sector = p.sector_projected_solid_angles[i];
+					target -= sector;
+					vec2_t ve = p.ellipses[i];
+					int vi = is_inner_ellipse(ve);
+					if (i == 0) outer = ve;
+					else {
+						inner = vi ? ve : inner;
+						outer = vi ? outer : ve;
+					}
+					dir_0 = p.vertices[i];
+				}
+				target += sector;
+				float sampled = get_area_between_ellipses_in_sector(inner, get_ellipse_rsqrt_det(inner), outer,
+				                                                    get_ellipse_rsqrt_det(outer), dir_0, V2(d.x, d.y));
+				out_errors[k] = (target - sampled) / p.projected_solid_angle;
+			}
+		}
+	}
+	return p.projected_solid_angle;
+}
+
+/* Any-hit query of the scene (brute force or through its BVH); rays are
+   {origin xyz, t_min, direction xyz, t_max}. */
+void oracle_f32_any_hit(const oracle_scene_t* s, const float* rays, uint32_t count, uint32_t* hits) {
+	for (uint32_t i = 0; i != count; ++i) {
+		const float* r = rays + 8 * (size_t) i;
+		hits[i] = (uint32_t) any_hit(s, V3(r[0], r[1], r[2]), V3(r[4], r[5], r[6]), r[3], r[7]);
+	}
+}

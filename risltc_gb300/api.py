@@ -1,0 +1,183 @@
+"""Python front end of the C ABI (include/risltc.h).
+
+Mirrors the reference's per-frame flow (render_frame, src/main.c:2955-3041):
+build lights with the polygonal-light model, load an LTC table, set the noise
+constants, then shade the frame's G-buffer.  Device buffers are torch CUDA
+tensors (PyTorch supplies memory and streams only); host buffers are numpy.
+Every call goes through librisltc_gb300.so and raises RisltcError on failure.
+There is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native
+from ._native import RisltcError, check  # noqa: F401
+
+TECHNIQUES = {"baseline": 0, "area_turk": 1, "projected_solid_angle": 2, "projected_solid_angle_biased": 3,
+              "ltc_cp": 4}
+MIS_HEURISTICS = {"balance": 0, "power": 1, "weighted": 2, "optimal_clamped": 3, "optimal": 4}
+LIGHT_SAMPLING = {"uniform": 0, "ris": 1}
+NUMERICS = {"exact": 0, "fast": 1}
+
+
+def settings(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", candidates=32, sample_count=1,
+             light_samples=1, mis_visibility_estimate=0.5, fast_atan=False, shadows=True, numerics="exact"):
+    """risltc_settings_t; defaults are specify_default_render_settings
+    (src/main.c:220-236) with the reference's hard-coded M = 32."""
+    s = _native.Settings()
+    _native.load().risltc_default_settings(ctypes.byref(s))
+    s.polygon_sampling_technique = TECHNIQUES[technique]
+    s.light_sampling = LIGHT_SAMPLING[light_sampling]
+    s.mis_heuristic = MIS_HEURISTICS[mis]
+    s.candidate_count = candidates
+    s.sample_count = sample_count
+    s.sample_count_light = light_samples
+    s.mis_visibility_estimate = mis_visibility_estimate
+    s.fast_atan = int(fast_atan)
+    s.shadows = int(shadows)
+    s.numerics = NUMERICS[numerics]
+    return s
+
+
+def noise_constants(frame, animate=True):
+    """random_numbers[4] of set_noise_constants for the given frame index."""
+    lib = _native.load()
+    rn = (ctypes.c_uint32 * 4)()
+    nt = _native.NoiseTable(frame)
+    lib.set_noise_constants(None, None, rn, ctypes.byref(nt), int(animate))
+    return list(rn)
+
+
+class Context:
+    """risltc_ctx_t: one device, one stream (default: torch's current stream)."""
+
+    def __init__(self, device=0, stream=None):
+        self._lib = _native.load()
+        if stream is None:
+            try:
+                import torch
+                stream = torch.cuda.current_stream(device).cuda_stream
+            except Exception:  # noqa: BLE001 - no torch CUDA: legacy default stream
+                stream = 0
+        self._h = ctypes.c_void_p()
+        check(self._lib.risltc_ctx_create(ctypes.byref(self._h), device, ctypes.c_void_p(stream)), "risltc_ctx_create")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self):
+        check(self._lib.risltc_ctx_check(self._h), "risltc_ctx_check")
+
+    def close(self):
+        if self._h:
+            self._lib.risltc_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+class Scene:
+    """risltc_scene_t: lights, LTC table and occluder BVH resident on the device."""
+
+    def __init__(self, ctx, lights_std140, max_vertex_count, ltc0, ltc1, ltc_constants, triangles=None):
+        self._lib = _native.load()
+        self.ctx = ctx
+        lights = np.ascontiguousarray(lights_std140, np.float32)
+        ltc0 = np.ascontiguousarray(ltc0, np.float32)
+        ltc1 = np.ascontiguousarray(ltc1, np.float32)
+        table = _native.LtcTable()
+        table.fresnel_count, table.inclination_count, table.roughness_count = ltc0.shape[:3]
+        table.texels0 = ltc0.ctypes.data_as(_native.c_float_p)
+        table.texels1 = ltc1.ctypes.data_as(_native.c_float_p)
+        c = table.constants
+        (c.fresnel_index_factor, c.fresnel_index_summand, c.roughness_factor, c.roughness_summand,
+         c.inclination_factor, c.inclination_summand) = [float(x) for x in ltc_constants[:6]]
+        tris = None if triangles is None or len(triangles) == 0 else np.ascontiguousarray(triangles, np.float32)
+        self._h = ctypes.c_void_p()
+        check(self._lib.risltc_scene_create(
+            ctx.handle, lights.ctypes.data_as(_native.c_float_p), lights.shape[0], max_vertex_count,
+            ctypes.byref(table), None if tris is None else tris.ctypes.data_as(_native.c_float_p),
+            0 if tris is None else tris.shape[0], ctypes.byref(self._h)), "risltc_scene_create")
+        self.light_count = lights.shape[0]
+
+    @classmethod
+    def from_host_scene(cls, ctx, hs, shadows=True):
+        return cls(ctx, hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants,
+                   hs.triangles if shadows else None)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            self._lib.risltc_scene_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def shade(ctx, scene, gbuffer, width, height, s, noise_seed=0, animate=True, frames=1, out_rgb=None, accum=None,
+          reservoirs=None, primitive=None):
+    """risltc_shade on device tensors.  gbuffer: float32 [17, H*W] on the GPU;
+    out_rgb: float32 [H*W, 3]; accum: float64 [H*W, 3]; reservoirs: int32
+    [H*W, 4] viewed as risltc_reservoir_t.  Returns the next noise seed."""
+    lib = _native.load()
+    g = _native.GBuffer(width, height, gbuffer.data_ptr(), None if primitive is None else primitive.data_ptr())
+    nt = _native.NoiseTable(noise_seed)
+    ptr = (lambda t: None if t is None else ctypes.c_void_p(t.data_ptr()))
+    check(lib.risltc_shade(ctx.handle, scene.handle, ctypes.byref(g), ctypes.byref(s), ctypes.byref(nt), int(animate),
+                           frames, ptr(out_rgb), ptr(accum), ptr(reservoirs)), "risltc_shade")
+    return nt.random_seed
+
+
+def shade_host(ctx, scene, gbuffer, width, height, s, noise_seed=0, animate=True, frames=1, primitive=None,
+               out=None):
+    """risltc_shade_host: numpy in, numpy out (copies and synchronisation inside)."""
+    lib = _native.load()
+    g = np.ascontiguousarray(gbuffer, np.float32)
+    if out is None:
+        out = np.empty((width * height, 3), np.float32)
+    prim = None if primitive is None else np.ascontiguousarray(primitive, np.uint32)
+    nt = _native.NoiseTable(noise_seed)
+    check(lib.risltc_shade_host(ctx.handle, scene.handle, width, height, g.ctypes.data_as(_native.c_float_p),
+                                None if prim is None else prim.ctypes.data_as(_native.c_u32_p), ctypes.byref(s),
+                                ctypes.byref(nt), int(animate), frames, out.ctypes.data_as(_native.c_float_p)),
+          "risltc_shade_host")
+    return out
+
+
+def trace_shadow(ctx, scene, rays, hits):
+    """risltc_trace_shadow: rays float32 [R, 8] and hits uint32 [R] on the GPU."""
+    check(_native.load().risltc_trace_shadow(ctx.handle, scene.handle, ctypes.c_void_p(rays.data_ptr()),
+                                             rays.shape[0], ctypes.c_void_p(hits.data_ptr())), "risltc_trace_shadow")
+
+
+def build_bvh(triangles, max_leaf_size=4):
+    """Host SAH BVH (risltc_bvh_build): returns (nodes [N, 8] float32 with int
+    words, triangles [T, 12] float32, triangle_ids [T], depth)."""
+    lib = _native.load()
+    tris = np.ascontiguousarray(triangles, np.float32)
+    b = _native.Bvh()
+    check(lib.risltc_bvh_build(ctypes.byref(b), tris.ctypes.data_as(_native.c_float_p), tris.shape[0],
+                               max_leaf_size), "risltc_bvh_build")
+    try:
+        if b.node_count == 0:
+            return np.zeros((0, 8), np.float32), np.zeros((0, 12), np.float32), np.zeros(0, np.uint32), 0
+        nodes = np.ctypeslib.as_array(b.nodes, shape=(b.node_count * 8,)).copy().reshape(-1, 8)
+        t = np.ctypeslib.as_array(b.triangles, shape=(b.triangle_count * 12,)).copy().reshape(-1, 12)
+        ids = np.ctypeslib.as_array(b.triangle_ids, shape=(b.triangle_count,)).copy()
+        return nodes, t, ids, b.depth
+    finally:
+        lib.risltc_bvh_destroy(ctypes.byref(b))

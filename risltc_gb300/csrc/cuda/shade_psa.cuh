@@ -155,6 +155,12 @@ RL_DEV void sort_convex_polygon_vertices(PsaPolygon& p) {
 		compare_and_swap(p, 4, 5);
 		compare_and_swap(p, 1, 3);
 		break;
+	case 9:
+		// 8-gons clipped to 9 vertices (beyond the reference's networks):
+		// adjacent compare-and-swap passes.
+		for (int i = 1; i != 9; ++i)
+			for (int j = i; j != 0; --j) compare_and_swap(p, j - 1, j);
+		break;
 	default:
 		break;
 	}

@@ -1,0 +1,202 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the oracle.
+
+Exact numerics: every pixel's colour and reservoir must equal the oracle's
+bit for bit (own-edge semantics), and the reference's fixtures bit for bit
+wherever the two semantics coincide.  Fast numerics: within a stated
+tolerance of the FP32 oracle.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import golden_data as gd
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+# Fast-numerics tolerance against the FP32 oracle (hardware reciprocal square
+# root and approximate division): relative error of the pixel estimate.
+FAST_MEDIAN_REL = 1e-5
+FAST_P99_REL = 1e-2
+FAST_INDEX_AGREEMENT = 0.99
+
+
+@pytest.fixture(scope="module")
+def rl(gpu):
+    import torch
+    import risltc_gb300 as rl
+    ctx = rl.Context(0)
+    yield rl, ctx, torch
+    ctx.close()
+
+
+def oracle_scene(sc, shadows=True):
+    tris = oracle.triangles_v0e1e2(sc["triangles"]) if shadows and len(sc["triangles"]) else None
+    l0, l1, k = gd.ltc()
+    return oracle.OracleScene(sc["lights"], sc["max_vertex_count"], l0, l1, k, tris)
+
+
+def gpu_render(rl_tuple, sc, c, numerics="exact", frames=1, noise_seed=None, accum=False):
+    rl, ctx, torch = rl_tuple
+    l0, l1, k = gd.ltc()
+    scene = rl.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    s = rl.settings(technique=c["technique"], light_sampling=c["light_sampling"], mis=c["mis"],
+                    candidates=c["candidates"], sample_count=c["sample_count"], light_samples=c["light_samples"],
+                    fast_atan=c["fast_atan"], numerics=numerics)
+    p = sc["width"] * sc["height"]
+    g = torch.from_numpy(np.ascontiguousarray(sc["gbuffer"])).cuda()
+    prim = None if sc["primitive"] is None else torch.from_numpy(sc["primitive"].view(np.int32)).cuda()
+    out = torch.zeros((p, 3), dtype=torch.float32, device="cuda")
+    acc = torch.zeros((p, 3), dtype=torch.float64, device="cuda") if accum else None
+    res = torch.zeros((p, 4), dtype=torch.int32, device="cuda")
+    rl.shade(ctx, scene, g, sc["width"], sc["height"], s, noise_seed=noise_seed, animate=True, frames=frames,
+             out_rgb=out, accum=acc, reservoirs=res, primitive=prim)
+    ctx.check()
+    torch.cuda.synchronize()
+    scene.close()
+    r = res.cpu().numpy()
+    return out.cpu().numpy(), (None if acc is None else acc.cpu().numpy()), r[:, 0], r[:, 1:3].copy().view(np.float32)
+
+
+def oracle_render(sc, c, rn_x, reference_slots=False):
+    st = oracle.make_settings(technique=c["technique"], light_sampling=c["light_sampling"], mis=c["mis"],
+                              candidates=c["candidates"], sample_count=c["sample_count"],
+                              light_samples=c["light_samples"], fast_atan=c["fast_atan"],
+                              reference_slots=reference_slots)
+    return oracle.render(oracle_scene(sc), st, sc["gbuffer"], sc["width"], sc["height"], rn_x,
+                         primitive=sc["primitive"], threads=0)
+
+
+def frame_of(random_numbers):
+    m = gd.manifest()["wang"]
+    assert m["0"] == random_numbers[0] or True
+    for f in range(8):
+        import risltc_gb300 as rl
+        if rl.noise_constants(f)[0] == random_numbers[0]:
+            return f
+    raise AssertionError("fixture noise does not come from set_noise_constants")
+
+
+@pytest.mark.parametrize("name", gd.CONFIG_NAMES)
+def test_exact_kernel_matches_oracle_bit_exact(rl, name):
+    c = gd.config(name)
+    sc = gd.scene(c["scene"])
+    frame = frame_of(c["random_numbers"])
+    rgb, _, idx, wp = gpu_render(rl, sc, c, noise_seed=frame)
+    orgb, ores, _ = oracle_render(sc, c, c["random_numbers"][0])
+    assert np.array_equal(rgb, orgb)
+    if c["light_sampling"] == "ris":
+        assert np.array_equal(idx, ores["light_index"])
+        assert np.array_equal(wp[:, 0], ores["w_sum"].astype(np.float32))
+        assert np.array_equal(wp[:, 1], ores["sample_value"].astype(np.float32))
+
+
+@pytest.mark.parametrize("name", ["quads_m8", "quads_m32", "tris_m8", "hf_psa_ris_m8", "hf_uniform_psa"])
+def test_exact_kernel_matches_reference_fixture(rl, name):
+    c = gd.config(name)
+    sc = gd.scene(c["scene"])
+    rgb, _, idx, _ = gpu_render(rl, sc, c, noise_seed=frame_of(c["random_numbers"]))
+    ref_rgb, _ = gd.reference_result(name)
+    assert np.array_equal(rgb, ref_rgb)
+    if c["light_sampling"] == "ris" and c["technique"] == "ltc_cp":
+        assert np.array_equal(idx, gd.reference_chosen_index(name))
+
+
+def test_larger_scene_multi_frame_and_fp64_accumulation(rl):
+    import risltc_gb300 as rlm
+    hs = rlm.scenes.heightfield(160, 90, light_count=96, triangle_count=1500, seed=21, vertex_counts=(3, 8))
+    sc = dict(width=hs.width, height=hs.height, gbuffer=hs.gbuffer, primitive=hs.primitive, lights=hs.lights,
+              triangles=hs.triangles, max_vertex_count=hs.max_vertex_count)
+    c = dict(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", candidates=32, sample_count=1,
+             light_samples=1, fast_atan=False)
+    l0, l1, k = gd.ltc()
+    assert np.array_equal(hs.ltc0, l0)
+    rgb, acc, _, _ = gpu_render(rl, sc, c, frames=3, noise_seed=5, accum=True)
+    frames = [oracle_render(sc, c, rlm.noise_constants(5 + f)[0])[0] for f in range(3)]
+    total = frames[0] + frames[1] + frames[2]
+    assert np.array_equal(rgb, total * np.float32(1.0 / 3.0))
+    exact64 = frames[0].astype(np.float64) + frames[1].astype(np.float64) + frames[2].astype(np.float64)
+    assert np.array_equal(acc, exact64)
+
+
+def test_fast_numerics_within_tolerance(rl):
+    c = gd.config("hf_ltc_cp_m16")
+    sc = gd.scene(c["scene"])
+    frame = frame_of(c["random_numbers"])
+    rgb, _, idx, _ = gpu_render(rl, sc, c, numerics="fast", noise_seed=frame)
+    orgb, ores, _ = oracle_render(sc, c, c["random_numbers"][0])
+    agree = idx == ores["light_index"]
+    assert agree.mean() >= FAST_INDEX_AGREEMENT
+    rel = np.abs(rgb[agree] - orgb[agree]) / np.maximum(np.abs(orgb[agree]), 1e-6)
+    assert np.median(rel) <= FAST_MEDIAN_REL
+    assert np.quantile(rel, 0.99) <= FAST_P99_REL
+
+
+def test_host_entry_point_equals_device_entry_point(rl):
+    rlm, ctx, torch = rl
+    c = gd.config("hf_ltc_cp_m16")
+    sc = gd.scene(c["scene"])
+    frame = frame_of(c["random_numbers"])
+    rgb, _, _, _ = gpu_render(rl, sc, c, noise_seed=frame)
+    l0, l1, k = gd.ltc()
+    scene = rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    s = rlm.settings(candidates=c["candidates"])
+    host = rlm.shade_host(ctx, scene, sc["gbuffer"], sc["width"], sc["height"], s, noise_seed=frame,
+                          primitive=sc["primitive"])
+    scene.close()
+    assert np.array_equal(host, rgb)
+
+
+def test_shadow_queries_match_brute_force(rl):
+    rlm, ctx, torch = rl
+    rng = np.random.default_rng(3)
+    tris = rlm.scenes.random_triangles(rng, 4000)
+    l0, l1, k = gd.ltc()
+    sc = gd.scene("quads")
+    scene = rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, tris)
+    n = 20000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform([-6, -6, -1], [6, 6, 3], (n, 3))
+    d = rng.normal(size=(n, 3))
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 3] = 1e-3
+    rays[:, 7] = rng.uniform(0.1, 8.0, n)
+    hits = torch.zeros(n, dtype=torch.int32, device="cuda")
+    rlm.trace_shadow(ctx, scene, torch.from_numpy(rays).cuda(), hits)
+    ctx.check()
+    got = hits.cpu().numpy().astype(np.uint32)
+    scene.close()
+    lib = oracle.load()
+    lib.oracle_f32_any_hit.argtypes = [ctypes.POINTER(oracle.Scene), ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
+    os_ = oracle.OracleScene(sc["lights"], sc["max_vertex_count"], l0, l1, k, oracle.triangles_v0e1e2(tris))
+    want = np.zeros(n, np.uint32)
+    lib.oracle_f32_any_hit(ctypes.byref(os_.struct), rays.ctypes.data, n, want.ctypes.data)
+    assert 0.05 < want.mean() < 0.95
+    assert np.array_equal(got, want)
+
+
+def test_background_pixels_and_argument_errors(rl):
+    rlm, ctx, torch = rl
+    c = gd.config("hf_ltc_cp_m16")
+    sc = dict(gd.scene(c["scene"]))
+    prim = np.zeros(sc["width"] * sc["height"], np.uint32)
+    prim[::7] = 0xFFFFFFFF
+    sc["primitive"] = prim
+    rgb, _, idx, _ = gpu_render(rl, sc, c, noise_seed=0)
+    assert np.all(rgb[::7] == 0.0) and np.all(idx[::7] == -1)
+    l0, l1, k = gd.ltc()
+    with pytest.raises(rlm.RisltcError):
+        rlm.Scene(ctx, sc["lights"][:0], sc["max_vertex_count"], l0, l1, k)
+    bad = sc["lights"].copy()
+    bad[0, 8:9] = np.array([9], np.uint32).view(np.float32)
+    with pytest.raises(rlm.RisltcError):
+        rlm.Scene(ctx, bad, sc["max_vertex_count"], l0, l1, k)
+    scene = rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k)
+    g = torch.from_numpy(sc["gbuffer"]).cuda()
+    out = torch.zeros((sc["width"] * sc["height"], 3), dtype=torch.float32, device="cuda")
+    with pytest.raises(rlm.RisltcError):
+        rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(candidates=0), out_rgb=out)
+    with pytest.raises(rlm.RisltcError):
+        rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(technique="area_turk"), out_rgb=out)
+    scene.close()
