@@ -1,0 +1,309 @@
+"""Benchmark of the shading path on the shadowed single-frame workload.
+
+Workload: a 1920x1080 G-buffer of a seeded fBm heightfield, 1024 convex
+polygon lights with 3..8 vertices (areas log-uniform [0.01, 1]), 200k random
+occluder triangles (edge 0.05..0.5) in [-6, 6]^2 x [0, 2] behind a SAH BVH,
+plain LTC-RIS with M = 32 candidates, 4 samples per pixel.  One step shades
+one frame (4 spp) in one kernel launch.  Metric: pixel-samples per second
+(one sample = M candidates + the PSA/MIS shade with its shadow rays).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  N > 1 runs one process per GPU (torchrun),
+each shading its own frame (weak scaling, no data-path collective).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOAD = "shadowed single frame: 1920x1080 fBm heightfield, 1024 polygon lights (3-8 vertices), " \
+           "200k occluder triangles (SAH BVH), plain LTC-RIS M=32, 4 spp"
+METRIC = "Gsamples/s (plain LTC-RIS, shadowed 1080p frame, 1024 lights, M=32, 4 spp)"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--lights", type=int, default=1024)
+    p.add_argument("--triangles", type=int, default=200_000)
+    p.add_argument("--candidates", type=int, default=32)
+    p.add_argument("--spp", type=int, default=4)
+    p.add_argument("--numerics", choices=["exact", "fast"], default="fast")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def make_workload(a, seed=0):
+    from risltc_gb300 import scenes
+    return scenes.heightfield(a.width, a.height, light_count=a.lights, triangle_count=a.triangles, seed=seed,
+                              vertex_counts=(3, 8))
+
+
+# ----------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(device_index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.f.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        smax = max(float(r[2]) for r in rows)
+        power = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# --------------------------------------------------------------- CPU leg --
+def _pixel_subset(hs, count, seed):
+    """A 1-row G-buffer of `count` pixels drawn uniformly from the frame's
+    covered pixels (an unbiased sample of the per-pixel cost)."""
+    valid = np.flatnonzero(hs.primitive == 0) if hs.primitive is not None else np.arange(hs.pixels)
+    pick = np.sort(np.random.default_rng(seed).choice(valid, size=min(count, valid.size), replace=False))
+    return np.ascontiguousarray(hs.gbuffer[:, pick]), pick.size
+
+
+def cpu_sample(hs, a, seconds_target, threads=0, seed=1, count_ops=True, repeats=1):
+    """Times the FP32 oracle (the reference's routines restated in C99,
+    OpenMP over rows) on pixels drawn uniformly from the same frame, and
+    counts the algorithmic FP32 operations per pixel-sample with the
+    op-counting build of the same oracle."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from risltc_gb300 import api
+    nodes, tris, _, _ = api.build_bvh(hs.triangles)
+    osc = oracle.OracleScene(hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants, tris, nodes)
+    st = oracle.make_settings(candidates=a.candidates)
+    rn = api.noise_constants(0)[0]
+    nthreads = threads or oracle.max_threads()
+    # Rows of 256 pixels so OpenMP has rows to balance.
+    probe, n = _pixel_subset(hs, 256 * nthreads, seed)
+    _, _, t = oracle.render(osc, st, probe, 256, n // 256, rn, threads=nthreads, reservoirs=False)
+    want = int(256 * (n // 256) * seconds_target / max(t, 1e-3))
+    want = max(256, min(want // 256 * 256, hs.pixels // 256 * 256))
+    sample, n = _pixel_subset(hs, want, seed + 1)
+    rows = n // 256
+    times = []
+    for _ in range(repeats):
+        _, _, t = oracle.render(osc, st, sample[:, :rows * 256], 256, rows, rn, threads=nthreads, reservoirs=False)
+        times.append(t)
+    out = {"samples": rows * 256, "seconds": statistics.median(times), "times": times, "threads": nthreads}
+    if count_ops:
+        ops_g, m = _pixel_subset(hs, 1024, seed + 2)
+        ops = oracle.opcount(osc, st, ops_g, m, 1, rn, (0, 1))
+        out["flops_per_sample"] = ops["flops"] / m
+        out["ops"] = {k: v for k, v in ops.items() if k != "rgb"}
+    return out
+
+
+def run_reference(a, rank, world):
+    """--impl reference: the oracle port of the reference's shading routines
+    (FP32, C99, OpenMP over all host threads) on a bounded band per step."""
+    if rank != 0:
+        return
+    hs = make_workload(a)
+    # Warm-up steps are folded into the probe; each timed step re-renders the
+    # same uniformly drawn pixel sample.
+    info = cpu_sample(hs, a, seconds_target=min(a.cpu_seconds, 8.0), count_ops=False, repeats=a.steps)
+    value = info["samples"] / info["seconds"] / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gsamples/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * info["seconds"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": "%d pixels drawn uniformly from the frame, 1 spp" % (
+            info["samples"])},
+        "cpu_baseline": {"value": value, "unit": "Gsamples/s", "cores": info["threads"], "kind": "port",
+                         "sample": "%d pixel-samples drawn uniformly from the frame per step, FP32 oracle "
+                                   "(C99, OpenMP)" % info["samples"]},
+        "e2e": {"value": value, "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU leg --
+def run_ours(a, rank, world, local_rank):
+    import torch
+    import risltc_gb300 as rl
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    hs = make_workload(a, seed=0)
+    P = hs.pixels
+    samples_per_step = int((hs.primitive == 0).sum() if hs.primitive is not None else P) * a.spp
+    ctx = rl.Context(local_rank)
+    scene = rl.Scene.from_host_scene(ctx, hs)
+    s = rl.settings(candidates=a.candidates, numerics=a.numerics)
+    g = torch.from_numpy(hs.gbuffer).cuda()
+    prim = torch.from_numpy(hs.primitive.view(np.int32)).cuda()
+    out = torch.empty((P, 3), dtype=torch.float32, device="cuda")
+    # Each rank shades different frames (its own noise seeds).
+    seed = rank * 1_000_000
+    for _ in range(a.warmup):
+        seed = rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, out_rgb=out,
+                        primitive=prim)
+    ctx.check()
+    clocks = ClockSampler(local_rank) if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(a.steps):
+        seed = rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, out_rgb=out,
+                        primitive=prim)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clock_info = clocks.stop() if clocks else None
+    ctx.check()
+    elapsed = start.elapsed_time(stop) / 1000.0
+    t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    elapsed = float(t.item())
+    value = samples_per_step * world * a.steps / elapsed / 1e9
+    ms_per_step = 1000.0 * elapsed / a.steps
+    result = {"value": value, "ms_per_step": ms_per_step}
+
+    # End to end through the host entry point: pinned G-buffer in, RGB out.
+    e2e = None
+    if not a.no_e2e:
+        hg = torch.from_numpy(hs.gbuffer).pin_memory()
+        hp = torch.from_numpy(hs.primitive.view(np.int32)).pin_memory()
+        ho = torch.empty((P, 3), dtype=torch.float32).pin_memory()
+        hgn, hpn, hon = hg.numpy(), hp.numpy().view(np.uint32), ho.numpy()
+        for _ in range(max(1, a.warmup // 2)):
+            rl.shade_host(ctx, scene, hgn, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, primitive=hpn,
+                          out=hon)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            rl.shade_host(ctx, scene, hgn, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, primitive=hpn,
+                          out=hon)
+            seed += a.spp
+        te = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device="cuda")
+        if dist:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e = {"value": samples_per_step * world * a.steps / float(te.item()) / 1e9, "unit": "Gsamples/s",
+               "h2d_bytes_per_step": int(hs.gbuffer.nbytes + hs.primitive.nbytes),
+               "d2h_bytes_per_step": int(P * 3 * 4)}
+    scene.close()
+    ctx.close()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peaks = measured_peaks()
+    props = torch.cuda.get_device_properties(local_rank)
+    sms = props.multi_processor_count
+    sm_max = peaks.get("sm_max_mhz") or (clock_info or {}).get("sm_max_mhz") or 2070.0
+    fp32_peak = 2.0 * 128 * sms * sm_max * 1e6 / 1e12  # TFLOP/s, 128 FP32 lanes per SM
+    cpu = None
+    flops_per_sample = None
+    if not a.no_cpu_baseline:
+        info = cpu_sample(hs, a, a.cpu_seconds)
+        flops_per_sample = info["flops_per_sample"]
+        cpu = {"value": info["samples"] / info["seconds"] / 1e9, "unit": "Gsamples/s", "cores": info["threads"],
+               "kind": "port", "sample": "%d pixel-samples drawn uniformly from the same frame at 1 spp, FP32 "
+                                         "oracle (C99, OpenMP over rows of 256)" % info["samples"]}
+    kernel_s = elapsed / a.steps  # one kernel launch per step
+    roofline = None
+    if flops_per_sample:
+        achieved = flops_per_sample * samples_per_step / kernel_s / 1e12
+        roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                    "frac": achieved / fp32_peak, "traffic": None,
+                    "kernel": "risltc::shade_kernel<%sNumerics>" % ("Fast" if a.numerics == "fast" else "Exact"),
+                    "flops_per_sample": flops_per_sample,
+                    "peak_source": "derived: 2 x 128 FP32 lanes x %d SMs x %.0f MHz (max SM clock of "
+                                   "MEASURED_PEAKS.json); no measured FP32 peak exists" % (sms, sm_max)}
+    line = {
+        "metric": METRIC, "value": result["value"], "unit": "Gsamples/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": result["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "width": hs.width, "height": hs.height, "lights": hs.light_count,
+                   "triangles": int(hs.triangles.shape[0]), "candidates": a.candidates, "spp": a.spp,
+                   "numerics": a.numerics, "samples_per_step": samples_per_step,
+                   "l2": "inputs larger than L2 (G-buffer %.0f MB > 129 MB)" % (hs.gbuffer.nbytes / 1e6),
+                   "parallelism": "one frame per GPU" if world > 1 else "single GPU"},
+        "gpu_launches": a.steps,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clock_info,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+    else:
+        run_ours(a, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -146,5 +146,44 @@ def render(scene, settings, gbuffer, width, height, random_number_x, primitive=N
     return rgb, res, seconds.value
 
 
+class OpCounts(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("add", "mul", "fma", "div", "sqrt", "atan", "sincos", "acos", "cmp")]
+
+
+# FP32 operations inside one call of each transcendental of include/risltc_math.h
+# (its polynomial evaluation plus reduction), counted from the source.
+TRANSCENDENTAL_FLOPS = {"atan": 24, "sincos": 30, "acos": 29}
+
+_oplib = None
+
+
+def opcount(scene, settings, gbuffer, width, height, random_number_x, rows, primitive=None):
+    """Renders rows with the op-counting oracle; returns a dict of tallies
+    and 'flops' = add + mul + 2 fma + div + sqrt + transcendental flops."""
+    global _oplib
+    if _oplib is None:
+        build_oracle.build()
+        _oplib = ctypes.CDLL(build_oracle.OPCOUNT_LIB)
+        _oplib.oracle_opcount_render.argtypes = [ctypes.POINTER(Scene), ctypes.POINTER(Settings),
+                                                 ctypes.POINTER(GBuffer), ctypes.c_uint32, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(OpCounts)]
+    g = GBuffer()
+    g.width, g.height = width, height
+    gbuffer = np.ascontiguousarray(gbuffer, np.float32)
+    g.planes = gbuffer.ctypes.data
+    prim = None if primitive is None else np.ascontiguousarray(primitive, np.uint32)
+    g.primitive = None if prim is None else prim.ctypes.data
+    rgb = np.zeros((width * height, 3), np.float32)
+    c = OpCounts()
+    if _oplib.oracle_opcount_render(ctypes.byref(scene.struct), ctypes.byref(settings), ctypes.byref(g),
+                                    random_number_x, rows[0], rows[1], rgb.ctypes.data, ctypes.byref(c)) != 0:
+        raise RuntimeError("op-count render failed")
+    d = {k: int(getattr(c, k)) for k, _ in OpCounts._fields_}
+    d["flops"] = (d["add"] + d["mul"] + 2 * d["fma"] + d["div"] + d["sqrt"]
+                  + sum(d[k] * v for k, v in TRANSCENDENTAL_FLOPS.items()))
+    d["rgb"] = rgb
+    return d
+
+
 def max_threads():
     return load().oracle_max_threads()

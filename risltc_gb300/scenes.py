@@ -220,7 +220,7 @@ def _heightfield_waves(rng, octaves=4):
 
 def _height(waves, x, y):
     h = np.zeros_like(x)
-    for a, fx, fy, ph in waves:
+    for a, fx, fy, ph in waves.astype(x.dtype):
         h += a * np.sin(fx * x + fy * y + ph)
     return h
 
@@ -256,12 +256,18 @@ def heightfield(width=1920, height=1080, light_count=1024, triangle_count=200_00
     t_lo = (cam[2] - hmax) / -dz
     t_hi = (cam[2] + hmax) / -dz
 
+    d32 = d.astype(np.float32)
+    cam32 = cam.astype(np.float32)
+
     def g(t):
-        p = cam[None, :] + t[:, None] * d
-        return p[:, 2] - _height(waves, p[:, 0], p[:, 1])
+        t = t.astype(np.float32)
+        x = cam32[0] + t * d32[:, 0]
+        y = cam32[1] + t * d32[:, 1]
+        z = cam32[2] + t * d32[:, 2]
+        return z - _height(waves, x, y)
 
     # Coarse march for the first sign change, then bisection.
-    steps = 16
+    steps = 10
     a = t_lo.copy()
     b = t_hi.copy()
     found = np.zeros(a.shape, bool)
@@ -273,7 +279,7 @@ def heightfield(width=1920, height=1080, light_count=1024, triangle_count=200_00
         b = np.where(below, t, b)
         found |= below
         prev_t = t
-    for _ in range(14):
+    for _ in range(12):
         m = 0.5 * (a + b)
         below = g(m) <= 0.0
         b = np.where(below, m, b)
