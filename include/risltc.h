@@ -272,6 +272,15 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
                                  uint32_t triangle_count, risltc_scene_t** scene);
 EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene);
 
+/* Sizes the context's scratch for frames of width x height pixels and
+ * frame_count frames per call: 16 bytes per pixel and frame of reservoir
+ * records between the candidate and shading kernels (used by the default
+ * configuration: LTC-CP, light_reservoir, one light sample).  risltc_shade
+ * grows the scratch itself when needed (a device allocation); calling this
+ * first keeps later risltc_shade calls free of allocations, e.g. for stream
+ * capture into a CUDA graph. */
+EXTERN_C int risltc_ctx_reserve(risltc_ctx_t* ctx, uint32_t width, uint32_t height, uint32_t frame_count);
+
 /* Shades frame_count consecutive frames of the G-buffer (device pointers).
  * Frame f uses the noise constants of set_noise_constants(..., noise,
  * animate) called once per frame (noise->random_seed advances by

@@ -92,6 +92,7 @@ SIGNATURES = {
     "risltc_default_settings": (None, [ctypes.POINTER(Settings)]),
     "risltc_ctx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]),
     "risltc_ctx_destroy": (None, [ctypes.c_void_p]),
+    "risltc_ctx_reserve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]),
     "risltc_scene_create": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_uint32, ctypes.c_uint32,
                                            ctypes.POINTER(LtcTable), c_float_p, ctypes.c_uint32,
                                            ctypes.POINTER(ctypes.c_void_p)]),

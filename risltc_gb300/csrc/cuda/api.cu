@@ -4,13 +4,15 @@
 #include <cstring>
 #include <vector>
 #include <cuda_runtime.h>
-#include "shade_kernel.cuh"
+#include "ris_kernels.cuh"
 
 namespace risltc {
 cudaError_t launch_shade_exact(const ShadeParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_shade_fast(const ShadeParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,
                                cudaStream_t stream, int grid);
+cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_ris_fast(const RisParams& p, cudaStream_t stream, int grid);
 }  // namespace risltc
 
 struct risltc_ctx_s {
@@ -24,6 +26,9 @@ struct risltc_ctx_s {
 	float* d_rgb;
 	size_t pixel_capacity;
 	float* h_pinned_rgb;
+	// Reservoir records between the candidate and shading kernels.
+	risltc::ReservoirRecord* d_records;
+	size_t record_capacity;
 };
 
 struct risltc_scene_s {
@@ -88,6 +93,7 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFree(ctx->d_primitive);
 	cudaFree(ctx->d_rgb);
 	cudaFreeHost(ctx->h_pinned_rgb);
+	cudaFree(ctx->d_records);
 	free(ctx);
 }
 
@@ -237,11 +243,59 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 	p.reservoirs = reservoirs;
 	p.error = ctx->d_error;
 	cudaSetDevice(ctx->device);
-	int grid = grid_for(ctx, (size_t) gbuffer->width * gbuffer->height);
-	cudaError_t e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_shade_fast(p, ctx->stream, grid)
-	                                                             : risltc::launch_shade_exact(p, ctx->stream, grid);
+	const size_t pixels = (size_t) gbuffer->width * gbuffer->height;
+	int grid = grid_for(ctx, pixels);
+	cudaError_t e;
+	if (settings->polygon_sampling_technique == sample_polygon_ltc_cp && settings->light_sampling == light_reservoir &&
+	    settings->sample_count_light == 1) {
+		// The reference's default configuration: candidate and shading
+		// kernels with reservoir records in between.
+		st = risltc_ctx_reserve(ctx, gbuffer->width, gbuffer->height, frame_count);
+		if (st) return st;
+		risltc::RisParams r;
+		memset(&r, 0, sizeof(r));
+		r.scene = p.scene;
+		r.gbuffer = p.gbuffer;
+		r.primitive = p.primitive;
+		r.width = p.width;
+		r.height = p.height;
+		r.candidate_count = p.candidate_count;
+		r.mis_heuristic = p.mis_heuristic;
+		r.sample_count = p.sample_count;
+		r.mis_visibility_estimate = p.mis_visibility_estimate;
+		r.fast_atan = p.fast_atan;
+		r.shadows = p.shadows;
+		r.noise_seed = p.noise_seed;
+		r.animate = p.animate;
+		r.frame_count = p.frame_count;
+		r.records = ctx->d_records;
+		r.out_rgb = out_rgb;
+		r.accum = accum;
+		r.reservoirs = reservoirs;
+		r.error = ctx->d_error;
+		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_ris_fast(r, ctx->stream, grid)
+		                                                 : risltc::launch_ris_exact(r, ctx->stream, grid);
+	} else {
+		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_shade_fast(p, ctx->stream, grid)
+		                                                 : risltc::launch_shade_exact(p, ctx->stream, grid);
+	}
 	if (e != cudaSuccess) return cuda_status(e);
 	noise->random_seed += frame_count;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_ctx_reserve(risltc_ctx_t* ctx, uint32_t width, uint32_t height, uint32_t frame_count) {
+	if (!ctx || width == 0 || height == 0 || frame_count == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
+	size_t need = (size_t) width * height * frame_count;
+	if (need <= ctx->record_capacity) return RISLTC_OK;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_records);
+	ctx->d_records = nullptr;
+	ctx->record_capacity = 0;
+	cudaError_t e = cudaMalloc(&ctx->d_records, need * sizeof(risltc::ReservoirRecord));
+	if (e != cudaSuccess) return cuda_status(e);
+	ctx->record_capacity = need;
 	return RISLTC_OK;
 }
 
