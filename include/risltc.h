@@ -145,7 +145,8 @@ enum risltc_status_e {
 	RISLTC_ERROR_NO_DEVICE = 6,
 	RISLTC_ERROR_OUT_OF_MEMORY = 7,
 	RISLTC_ERROR_IO = 8,
-	RISLTC_ERROR_UNSUPPORTED = 9
+	RISLTC_ERROR_UNSUPPORTED = 9,
+	RISLTC_ERROR_TOO_LARGE = 10
 };
 
 /* Largest light vertex count (MAX_POLYGONAL_LIGHT_VERTEX_COUNT of
@@ -300,6 +301,34 @@ EXTERN_C int risltc_shade_host(risltc_ctx_t* ctx, const risltc_scene_t* scene, u
                                const float* gbuffer_planes, const uint32_t* primitive,
                                const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
                                uint32_t frame_count, float* out_rgb);
+
+/* Allocation-free shading, for callers that may not allocate device memory
+ * while they render: a plugin inside a host application that owns the device
+ * memory budget (a game engine or content-creation tool with its own
+ * allocator), or a frame loop that must not stall other streams (cudaMalloc
+ * and cudaFree synchronise the device).  Such a caller creates the scene once,
+ * where allocation is allowed, and shades each frame here.  No counterpart in
+ * the reference, which renders through Vulkan.
+ *
+ * Same arguments and results as risltc_shade for the default configuration
+ * (LTC-CP technique, light_reservoir, one light sample; other settings return
+ * RISLTC_ERROR_UNSUPPORTED), on the given CUDA stream (NULL: the legacy
+ * default stream) of the current device, but without a context: the
+ * reservoir records between the two kernels and the error word live in a
+ * static device array of RISLTC_NOALLOC_MAX_PIXEL_FRAMES records (4 MiB),
+ * which every GPU that loads the library holds until the process exits.
+ * width * height * frame_count above that limit returns
+ * RISLTC_ERROR_TOO_LARGE before any work.  The call waits for its stream to
+ * finish and returns the kernels' error status.  The first call on each
+ * device resolves the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (other streams, other threads) race, so serialise
+ * them. */
+#define RISLTC_NOALLOC_MAX_PIXEL_FRAMES 262144
+EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                                  const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
+                                  uint32_t frame_count, float* out_rgb, double* accum,
+                                  risltc_reservoir_t* reservoirs, void* stream);
 
 /* Any-hit shadow queries through the scene BVH: rays are 8 floats
    {origin xyz, t_min, direction xyz, t_max} in device memory; hits gets

@@ -103,6 +103,9 @@ SIGNATURES = {
     "risltc_shade_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
                                          c_float_p, c_u32_p, ctypes.POINTER(Settings), ctypes.POINTER(NoiseTable),
                                          ctypes.c_uint32, ctypes.c_uint32, c_float_p]),
+    "risltc_shade_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GBuffer), ctypes.POINTER(Settings),
+                                            ctypes.POINTER(NoiseTable), ctypes.c_uint32, ctypes.c_uint32,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "risltc_trace_shadow": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                            ctypes.c_void_p]),
     "risltc_ctx_check": (ctypes.c_int, [ctypes.c_void_p]),

@@ -21,6 +21,7 @@ CUDA_SOURCES = {
     "cuda/shade_exact.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "cuda/shade_fast.cu": ["--fmad=true", "-prec-div=true", "-prec-sqrt=true"],
     "cuda/api.cu": [],
+    "cuda/noalloc.cu": [],
 }
 
 

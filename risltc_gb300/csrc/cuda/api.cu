@@ -185,6 +185,9 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	return RISLTC_OK;
 }
 
+// The device view of a scene, for the allocation-free entry point (noalloc.cu).
+risltc::SceneView risltc_scene_view(const risltc_scene_t* scene) { return scene->view; }
+
 EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene) {
 	if (!scene) return;
 	cudaSetDevice(scene->ctx->device);
@@ -377,6 +380,7 @@ EXTERN_C const char* risltc_status_string(int status) {
 	case RISLTC_ERROR_OUT_OF_MEMORY: return "out of memory";
 	case RISLTC_ERROR_IO: return "file could not be read";
 	case RISLTC_ERROR_UNSUPPORTED: return "unsupported setting";
+	case RISLTC_ERROR_TOO_LARGE: return "frame larger than the static scratch of risltc_shade_noalloc";
 	default: return "unknown status";
 	}
 }
