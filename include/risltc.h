@@ -336,6 +336,15 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene, const float* rays, uint32_t ray_count,
                                  uint32_t* hits);
 
+/* Kernel timing with CUDA events on the context's stream.  Returns the time
+ * of the shading calls made since the previous call of this function (at
+ * most 64 calls are timed), split into phase_ms[0] (the RIS candidate kernel,
+ * or the fused kernel) and phase_ms[1] (the shading kernel; 0 for the fused
+ * kernel), and their number in calls; then enables (enable != 0) or disables
+ * timing of the following calls.  phase_ms and calls may be NULL.  Querying
+ * synchronises the stream. */
+EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, uint32_t* calls);
+
 /* Synchronises the context's stream and returns the first error recorded by
    a kernel since the last check (RISLTC_OK if none). */
 EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx);

@@ -108,6 +108,7 @@ SIGNATURES = {
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "risltc_trace_shadow": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                            ctypes.c_void_p]),
+    "risltc_ctx_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_float_p, c_u32_p]),
     "risltc_ctx_check": (ctypes.c_int, [ctypes.c_void_p]),
     "risltc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
 }

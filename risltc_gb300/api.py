@@ -71,6 +71,15 @@ class Context:
     def check(self):
         check(self._lib.risltc_ctx_check(self._h), "risltc_ctx_check")
 
+    def profile(self, enable=True):
+        """Per-kernel CUDA-event times (ms) of the shading calls since the last
+        call: (candidate or fused kernel, shading kernel, number of calls);
+        then switches timing on or off."""
+        ms = (ctypes.c_float * 2)()
+        calls = ctypes.c_uint32(0)
+        check(self._lib.risltc_ctx_profile(self._h, int(enable), ms, ctypes.byref(calls)), "risltc_ctx_profile")
+        return float(ms[0]), float(ms[1]), int(calls.value)
+
     def close(self):
         if self._h:
             self._lib.risltc_ctx_destroy(self._h)

@@ -46,21 +46,25 @@ def _run(cmd):
     return proc.stderr
 
 
-def build(force=False, verbose=False):
-    """Compiles the library if any source is newer; returns its path."""
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in _deps())):
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, extra_flags=(), out=None):
+    """Compiles the library if any source is newer; returns its path.
+    extra_flags go to every nvcc command (e.g. -D tuning macros); out
+    redirects the library (and its objects) elsewhere."""
+    lib = out or LIB
+    build_dir = os.path.join(os.path.dirname(lib), "_build_" + os.path.basename(lib)) if out else BUILD
+    if (not force and os.path.exists(lib)
+            and os.path.getmtime(lib) >= max(os.path.getmtime(d) for d in _deps())):
+        return lib
+    os.makedirs(build_dir, exist_ok=True)
     jobs = []
     for src in HOST_SOURCES:
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         jobs.append((["gcc", "-std=c99", "-O3", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
                       "-c", os.path.join(CSRC, src), "-o", obj], obj))
     for src, flags in CUDA_SOURCES.items():
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-               "-Xptxas", "-v"] + ARCH + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
+               "-Xptxas", "-v"] + ARCH + flags + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
         jobs.append((cmd, obj))
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(lambda j: _run(j[0]), jobs))
@@ -69,9 +73,9 @@ def build(force=False, verbose=False):
             if log:
                 print(log)
     objs = [o for _, o in jobs]
-    _run([nvcc(), "-shared"] + ARCH + ["-o", LIB + ".tmp"] + objs + ["-lm"])
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    _run([nvcc(), "-shared"] + ARCH + ["-o", lib + ".tmp"] + objs + ["-lm"])
+    os.replace(lib + ".tmp", lib)
+    return lib
 
 
 if __name__ == "__main__":

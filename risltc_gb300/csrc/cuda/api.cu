@@ -7,12 +7,12 @@
 #include "ris_kernels.cuh"
 
 namespace risltc {
-cudaError_t launch_shade_exact(const ShadeParams& p, cudaStream_t stream, int grid);
-cudaError_t launch_shade_fast(const ShadeParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_shade_exact(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
+cudaError_t launch_shade_fast(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
 cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,
                                cudaStream_t stream, int grid);
-cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid);
-cudaError_t launch_ris_fast(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
+cudaError_t launch_ris_fast(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
 }  // namespace risltc
 
 struct risltc_ctx_s {
@@ -29,6 +29,12 @@ struct risltc_ctx_s {
 	// Reservoir records between the candidate and shading kernels.
 	risltc::ReservoirRecord* d_records;
 	size_t record_capacity;
+	// Kernel timing: three events per shading call (before, between and
+	// after the two phases), up to kTimedCalls calls between queries.
+	int profiling;
+	int timed_calls;
+	cudaEvent_t events[64][3];
+	int events_created;
 };
 
 struct risltc_scene_s {
@@ -94,6 +100,8 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFree(ctx->d_rgb);
 	cudaFreeHost(ctx->h_pinned_rgb);
 	cudaFree(ctx->d_records);
+	for (int i = 0; i < ctx->events_created; ++i)
+		for (int k = 0; k != 3; ++k) cudaEventDestroy(ctx->events[i][k]);
 	free(ctx);
 }
 
@@ -105,7 +113,7 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 		return RISLTC_ERROR_INVALID_ARGUMENT;
 	*out = nullptr;
 	cudaSetDevice(ctx->device);
-	// Lights: 128-byte records {radiance, vertex_count | plane | 8 vertices xyz}.
+	// Lights: 160-byte records {radiance, vertex_count | plane | 8 x {xyz, 0}}.
 	const size_t stride = 12 + 4 * (size_t) max_vertex_count;
 	std::vector<float> lights((size_t) light_count * risltc::kLightWords, 0.0f);
 	for (uint32_t i = 0; i != light_count; ++i) {
@@ -121,9 +129,10 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 		for (int c = 0; c != 4; ++c) d[4 + c] = s[4 + c];
 		for (uint32_t v = 0; v != RISLTC_MAX_LIGHT_VERTEX_COUNT; ++v) {
 			const float* src = s + 12 + 4 * (v < vc ? v : 0);
-			d[8 + 3 * v + 0] = src[0];
-			d[8 + 3 * v + 1] = src[1];
-			d[8 + 3 * v + 2] = src[2];
+			d[8 + 4 * v + 0] = src[0];
+			d[8 + 4 * v + 1] = src[1];
+			d[8 + 4 * v + 2] = src[2];
+			d[8 + 4 * v + 3] = 0.0f;
 		}
 	}
 	// LTC: 8 floats per texel {m00, -m02, m11, m20, m22, albedo, 0, 0}.
@@ -249,6 +258,15 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 	const size_t pixels = (size_t) gbuffer->width * gbuffer->height;
 	int grid = grid_for(ctx, pixels);
 	cudaError_t e;
+	cudaEvent_t* events = nullptr;
+	if (ctx->profiling && ctx->timed_calls < 64) {
+		int i = ctx->timed_calls++;
+		if (i >= ctx->events_created) {
+			for (int k = 0; k != 3; ++k) cudaEventCreate(&ctx->events[i][k]);
+			ctx->events_created = i + 1;
+		}
+		events = ctx->events[i];
+	}
 	if (settings->polygon_sampling_technique == sample_polygon_ltc_cp && settings->light_sampling == light_reservoir &&
 	    settings->sample_count_light == 1) {
 		// The reference's default configuration: candidate and shading
@@ -276,11 +294,11 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		r.accum = accum;
 		r.reservoirs = reservoirs;
 		r.error = ctx->d_error;
-		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_ris_fast(r, ctx->stream, grid)
-		                                                 : risltc::launch_ris_exact(r, ctx->stream, grid);
+		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_ris_fast(r, ctx->stream, grid, events)
+		                                                 : risltc::launch_ris_exact(r, ctx->stream, grid, events);
 	} else {
-		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_shade_fast(p, ctx->stream, grid)
-		                                                 : risltc::launch_shade_exact(p, ctx->stream, grid);
+		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_shade_fast(p, ctx->stream, grid, events)
+		                                                 : risltc::launch_shade_exact(p, ctx->stream, grid, events);
 	}
 	if (e != cudaSuccess) return cuda_status(e);
 	noise->random_seed += frame_count;
@@ -350,6 +368,29 @@ EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene,
 	cudaError_t e = risltc::launch_trace_exact(scene->view, (const float4*) rays, ray_count, hits, ctx->d_error,
 	                                           ctx->stream, grid_for(ctx, ray_count));
 	return cuda_status(e);
+}
+
+EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, uint32_t* calls) {
+	if (!ctx) return RISLTC_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(ctx->device);
+	int status = RISLTC_OK;
+	if (phase_ms) {
+		phase_ms[0] = phase_ms[1] = 0.0f;
+		cudaError_t e = cudaStreamSynchronize(ctx->stream);
+		if (e != cudaSuccess) return cuda_status(e);
+		for (int i = 0; i != ctx->timed_calls; ++i) {
+			float a = 0.0f, b = 0.0f;
+			if (cudaEventElapsedTime(&a, ctx->events[i][0], ctx->events[i][1]) != cudaSuccess ||
+			    cudaEventElapsedTime(&b, ctx->events[i][1], ctx->events[i][2]) != cudaSuccess)
+				status = RISLTC_ERROR_CUDA;
+			phase_ms[0] += a;
+			phase_ms[1] += b;
+		}
+	}
+	if (calls) *calls = (uint32_t) ctx->timed_calls;
+	ctx->timed_calls = 0;
+	ctx->profiling = enable;
+	return status;
 }
 
 EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx) {

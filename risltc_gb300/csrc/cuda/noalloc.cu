@@ -17,8 +17,8 @@
 risltc::SceneView risltc_scene_view(const risltc_scene_t* scene);
 
 namespace risltc {
-cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid);
-cudaError_t launch_ris_fast(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
+cudaError_t launch_ris_fast(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
 }  // namespace risltc
 
 // The scratch: reservoir records for up to RISLTC_NOALLOC_MAX_PIXEL_FRAMES
@@ -103,8 +103,8 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 	size_t blocks = ((size_t) gbuffer->width * gbuffer->height + 127) / 128;
 	if (blocks > (size_t) sms * 16) blocks = (size_t) sms * 16;
-	e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_ris_fast(r, s, (int) blocks)
-	                                                 : risltc::launch_ris_exact(r, s, (int) blocks);
+	e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_ris_fast(r, s, (int) blocks, nullptr)
+	                                                 : risltc::launch_ris_exact(r, s, (int) blocks, nullptr);
 	if (e != cudaSuccess) return to_status(e);
 	uint32_t bits = 0;
 	e = cudaMemcpyAsync(&bits, &scratch->error, sizeof(bits), cudaMemcpyDeviceToHost, s);

@@ -44,49 +44,61 @@ struct RisParams {
 	uint32_t* error;
 };
 
-// Sum of integrate_edge over the n edges of an unclipped polygon, in slot
-// order (calculate_ltc with vc == n), all indices static.
+// Sum of integrate_edge over the n edges of an unclipped polygon in slot
+// order (calculate_ltc with vc == n): edges 0..n-2, then the closing edge
+// n-1 -> 0.  All array indices are static.
 template <class P> RL_DEV float ltc_integral_unclipped(const f3 (&v)[kMaxLightVertices], uint32_t n) {
 	f3 nv[kMaxLightVertices];
 #pragma unroll
 	for (int i = 0; i != kMaxLightVertices; ++i) nv[i] = normalize<P>(v[i]);
+	f3 last = nv[2];
+#pragma unroll
+	for (int j = 3; j != kMaxLightVertices; ++j)
+		if (j + 1 == (int) n) last = nv[j];
 	float result = 0.0f;
 #pragma unroll
-	for (int i = 0; i != kMaxLightVertices; ++i) {
-		if (i < (int) n) {
-			f3 next = nv[0];
-#pragma unroll
-			for (int j = 1; j != kMaxLightVertices; ++j)
-				if (j == i + 1 && j < (int) n) next = nv[j];
-			result += integrate_edge<P>(nv[i], next);
-		}
-	}
+	for (int i = 0; i + 1 != kMaxLightVertices; ++i)
+		if (i + 1 < (int) n) result += integrate_edge<P>(nv[i], nv[i + 1]);
+	result += integrate_edge<P>(last, nv[0]);
 	return fabsf(result);
 }
 
+struct PolygonVerts {
+	f3 v[kMaxLightVertices];
+};
+
 // Partially clipped polygon: the general clipper and integral (about 1% of
-// candidates).  Returns -1 when the polygon clips to nothing.
-template <class P> __device__ __noinline__ float ltc_integral_clipped(const f3* v_in, uint32_t n) {
+// candidates).  Takes the vertices by value so the caller's copy can stay in
+// registers.  Returns -1 when the polygon clips to nothing.
+template <class P> __device__ __noinline__ float ltc_integral_clipped(PolygonVerts in, uint32_t n) {
 	f3 v[kMaxPolygonVertices];
-	for (int i = 0; i != kMaxLightVertices; ++i) v[i] = v_in[i];
+	for (int i = 0; i != kMaxLightVertices; ++i) v[i] = in.v[i];
 	uint32_t vc = clip_polygon<P>(n, v);
 	return vc > 0 ? calculate_ltc<P>(vc, v) : -1.0f;
 }
 
-// The LTC integral of one light transformed by m (mat4x3 * vec4(v, 1));
-// clipped_away reports a polygon entirely below the horizon.
-template <class P> RL_DEV float ltc_integral(const mat43& m, const Light& l, bool& clipped_away) {
-	f3 t[kMaxLightVertices];
+// The LTC integral of one light record's polygon transformed by m
+// (mat4x3 * vec4(v, 1)), with the y coordinate negated when flip_y is set;
+// clipped_away reports a polygon entirely below the horizon.  Negating the
+// transformed y equals transforming with the y row of m negated, bit for bit
+// (negation is exact and rounding symmetric): the side flip of
+// shading_pass.frag.glsl:424-428.  Vertices stream from the record.
+template <class P>
+RL_DEV float ltc_integral(const mat43& m, bool flip_y, const float4* record, uint32_t n, bool& clipped_away) {
+	PolygonVerts t;
 	uint32_t above = 0;
 #pragma unroll
 	for (int j = 0; j != kMaxLightVertices; ++j) {
-		t[j] = mul_point(m, l.v[j]);
-		if (j < (int) l.vertex_count && t[j].z > 0.0f) ++above;
+		// Slots past the count hold vertex 0, so they are always valid.
+		float4 q = __ldg(record + 2 + j);
+		t.v[j] = mul_point(m, mk3(q.x, q.y, q.z));
+		t.v[j].y = flip_y ? -t.v[j].y : t.v[j].y;
+		if (j < (int) n && t.v[j].z > 0.0f) ++above;
 	}
 	clipped_away = above == 0;
-	if (above == l.vertex_count) return ltc_integral_unclipped<P>(t, l.vertex_count);
+	if (above == n) return ltc_integral_unclipped<P>(t.v, n);
 	if (above == 0) return 0.0f;
-	float r = ltc_integral_clipped<P>(t, l.vertex_count);
+	float r = ltc_integral_clipped<P>(t, n);
 	clipped_away = r < 0.0f;
 	return clipped_away ? 0.0f : r;
 }
@@ -96,25 +108,40 @@ struct CandidateFrame {
 	f3 position;
 	f3 diffuse_albedo;
 	float ltc_albedo;
-	mat43 w2s[2];  // world to shading space, [1]: y row negated (the side flip)
-	mat43 w2c[2];  // shading_to_cosine * w2s[side]
+	mat43 w2s;     // world to shading space
+	mat43 w2c[2];  // shading_to_cosine * w2s, [1] with the y row of w2s negated
 };
 
 // evaluate_polygonal_light_shading with SAMPLE_POLYGON_LTC_CP,
-// shading_pass.frag.glsl:421-456, for one candidate light.
-template <class P> RL_DEV f3 ltc_cp_candidate(const CandidateFrame& cf, const Light& l) {
-	const int flip = plane_dot(cf.position, l.plane) < 0.0f ? 1 : 0;
+// shading_pass.frag.glsl:421-456, for one candidate light record.
+template <class P> RL_DEV f3 ltc_cp_candidate(const CandidateFrame& cf, const float4* record) {
+	float4 head = __ldg(record), pl = __ldg(record + 1);
+	const f3 radiance = mk3(head.x, head.y, head.z);
+	const uint32_t n = __float_as_uint(head.w);
+	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
+	const int flip = plane_dot(cf.position, plane) < 0.0f ? 1 : 0;
 	f3 result = splat(0.0f);
 	bool clipped_away;
-	float cd = ltc_integral<P>(cf.w2s[flip], l, clipped_away);
-	f3 diffuse = clipped_away ? splat(0.0f) : mul(scale(cf.diffuse_albedo, cd), l.radiance);
+	float cd = ltc_integral<P>(cf.w2s, flip != 0, record, n, clipped_away);
+	f3 diffuse = clipped_away ? splat(0.0f) : mul(scale(cf.diffuse_albedo, cd), radiance);
 	result = add(result, diffuse);
-	float cs = ltc_integral<P>(cf.w2c[flip], l, clipped_away);
-	f3 ggx = clipped_away ? splat(0.0f) : mul(splat(cs * cf.ltc_albedo), l.radiance);
+	mat43 w2c;
+#pragma unroll
+	for (int c = 0; c != 4; ++c) {
+		w2c.c[c].x = flip ? cf.w2c[1].c[c].x : cf.w2c[0].c[c].x;
+		w2c.c[c].y = flip ? cf.w2c[1].c[c].y : cf.w2c[0].c[c].y;
+		w2c.c[c].z = flip ? cf.w2c[1].c[c].z : cf.w2c[0].c[c].z;
+	}
+	float cs = ltc_integral<P>(w2c, false, record, n, clipped_away);
+	f3 ggx = clipped_away ? splat(0.0f) : mul(splat(cs * cf.ltc_albedo), radiance);
 	return add(result, ggx);
 }
 
-template <class P> __global__ void __launch_bounds__(128) ris_candidates_kernel(RisParams pr) {
+#ifndef RISLTC_CANDIDATE_MIN_BLOCKS
+#define RISLTC_CANDIDATE_MIN_BLOCKS 5
+#endif
+template <class P>
+__global__ void __launch_bounds__(128, RISLTC_CANDIDATE_MIN_BLOCKS) ris_candidates_kernel(RisParams pr) {
 	const uint32_t np = pr.width * pr.height;
 	const int n = pr.scene.light_count;
 	const float p = P::rcp((float) n);
@@ -138,12 +165,12 @@ template <class P> __global__ void __launch_bounds__(128) ris_candidates_kernel(
 			float fl = dot(fresnel_0, mk3(0.2126f, 0.7152f, 0.0722f));
 			Ltc ltc = get_ltc_coefficients<P>(pr.scene, fl, roughness, position, normal, outgoing);
 			cf.ltc_albedo = ltc.albedo;
-			cf.w2s[0] = ltc.world_to_shading;
-			cf.w2s[1] = ltc.world_to_shading;
+			cf.w2s = ltc.world_to_shading;
+			mat43 flipped = ltc.world_to_shading;
 #pragma unroll
-			for (int c = 0; c != 4; ++c) cf.w2s[1].c[c].y = -cf.w2s[1].c[c].y;
-			cf.w2c[0] = mul(ltc.shading_to_cosine, cf.w2s[0]);
-			cf.w2c[1] = mul(ltc.shading_to_cosine, cf.w2s[1]);
+			for (int c = 0; c != 4; ++c) flipped.c[c].y = -flipped.c[c].y;
+			cf.w2c[0] = mul(ltc.shading_to_cosine, cf.w2s);
+			cf.w2c[1] = mul(ltc.shading_to_cosine, flipped);
 		}
 		const uint32_t x = i % pr.width, y = i / pr.width;
 		for (uint32_t f = 0; f != pr.frame_count; ++f) {
@@ -154,9 +181,17 @@ template <class P> __global__ void __launch_bounds__(128) ris_candidates_kernel(
 			for (int c = 0; c != pr.candidate_count; ++c) {
 				int idx = (int) (get_noise_1(seed) * (float) n);
 				idx = idx > n - 1 ? n - 1 : idx;
-				Light l;
-				load_light(pr.scene, idx, l);
-				f3 color = ltc_cp_candidate<P>(cf, l);
+				{
+					// The next candidate's index is two LCG steps ahead: start
+					// pulling its record (two cache lines) into L1 now.
+					uint32_t ahead = 1664525u * (1664525u * seed + 1013904223u) + 1013904223u;
+					int next = (int) (__uint2float_rn(ahead) * 2.3283064365386962890625e-10f * (float) n);
+					next = next > n - 1 ? n - 1 : next;
+					const char* rec = (const char*) light_record(pr.scene, next);
+					asm volatile("prefetch.global.L1 [%0];" ::"l"(rec));
+					asm volatile("prefetch.global.L1 [%0];" ::"l"(rec + 128));
+				}
+				f3 color = ltc_cp_candidate<P>(cf, light_record(pr.scene, idx));
 				float p_hat = P::sqrt(dot(color, color));
 				float w = P::div(p_hat, p);
 				float rnd = get_noise_1(seed);
