@@ -142,9 +142,15 @@ def cpu_sample(hs, a, seconds_target, threads=0, seed=1, count_ops=True, repeats
         times.append(t)
     out = {"samples": rows * 256, "seconds": statistics.median(times), "times": times, "threads": nthreads}
     if count_ops:
+        # Counted with M and with one candidate: the difference is the
+        # candidate phase, the rest the final PSA/MIS shading.
         ops_g, m = _pixel_subset(hs, 1024, seed + 2)
         ops = oracle.opcount(osc, st, ops_g, m, 1, rn, (0, 1))
+        one = oracle.opcount(osc, oracle.make_settings(candidates=1), ops_g, m, 1, rn, (0, 1))
+        per_candidate = (ops["flops"] - one["flops"]) / m / max(a.candidates - 1, 1)
         out["flops_per_sample"] = ops["flops"] / m
+        out["candidate_flops_per_sample"] = per_candidate * a.candidates
+        out["shade_flops_per_sample"] = ops["flops"] / m - per_candidate * a.candidates
         out["ops"] = {k: v for k, v in ops.items() if k != "rgb"}
     return out
 
@@ -203,6 +209,7 @@ def run_ours(a, rank, world, local_rank):
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.profile(True)  # per-kernel CUDA events on the same stream
     start.record(stream)
     for _ in range(a.steps):
         seed = rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, out_rgb=out,
@@ -212,7 +219,21 @@ def run_ours(a, rank, world, local_rank):
     if dist:
         dist.barrier()
     clock_info = clocks.stop() if clocks else None
+    cand_ms, shade_ms, timed_calls = ctx.profile(False)
     ctx.check()
+    # The same step with exact numerics everywhere (bit-identical to the
+    # oracle), for reference.
+    exact_s = rl.settings(candidates=a.candidates, numerics="exact")
+    rl.shade(ctx, scene, g, hs.width, hs.height, exact_s, noise_seed=seed, frames=a.spp, out_rgb=out, primitive=prim)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        seed = rl.shade(ctx, scene, g, hs.width, hs.height, exact_s, noise_seed=seed, frames=a.spp, out_rgb=out,
+                        primitive=prim)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    exact_value = samples_per_step * a.steps / (e0.elapsed_time(e1) / 1000.0) / 1e9
     elapsed = start.elapsed_time(stop) / 1000.0
     t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
     if dist:
@@ -258,20 +279,28 @@ def run_ours(a, rank, world, local_rank):
     fp32_peak = 2.0 * 128 * sms * sm_max * 1e6 / 1e12  # TFLOP/s, 128 FP32 lanes per SM
     cpu = None
     flops_per_sample = None
+    info = {}
     if not a.no_cpu_baseline:
         info = cpu_sample(hs, a, a.cpu_seconds)
         flops_per_sample = info["flops_per_sample"]
         cpu = {"value": info["samples"] / info["seconds"] / 1e9, "unit": "Gsamples/s", "cores": info["threads"],
                "kind": "port", "sample": "%d pixel-samples drawn uniformly from the same frame at 1 spp, FP32 "
                                          "oracle (C99, OpenMP over rows of 256)" % info["samples"]}
-    kernel_s = elapsed / a.steps  # one kernel launch per step
     roofline = None
+    kernels = {"ris_candidates_kernel": {"ms_per_launch": cand_ms / max(timed_calls, 1)},
+               "ris_shade_kernel": {"ms_per_launch": shade_ms / max(timed_calls, 1)}}
     if flops_per_sample:
-        achieved = flops_per_sample * samples_per_step / kernel_s / 1e12
-        roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                    "frac": achieved / fp32_peak, "traffic": None,
-                    "kernel": "risltc::shade_kernel<%sNumerics>" % ("Fast" if a.numerics == "fast" else "Exact"),
-                    "flops_per_sample": flops_per_sample,
+        kernels["ris_candidates_kernel"]["flops_per_sample"] = info["candidate_flops_per_sample"]
+        kernels["ris_shade_kernel"]["flops_per_sample"] = info["shade_flops_per_sample"]
+        for k in kernels.values():
+            k["achieved_tflops"] = k["flops_per_sample"] * samples_per_step / (k["ms_per_launch"] / 1e3) / 1e12
+            k["frac"] = k["achieved_tflops"] / fp32_peak
+        dominant = max(kernels, key=lambda k: kernels[k]["ms_per_launch"])
+        d = kernels[dominant]
+        roofline = {"bound": "fp32", "achieved": d["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
+                    "frac": d["frac"], "traffic": None, "kernel": dominant,
+                    "flops_per_sample": d["flops_per_sample"],
+                    "whole_step_frac": flops_per_sample * samples_per_step / (elapsed / a.steps) / 1e12 / fp32_peak,
                     "peak_source": "derived: 2 x 128 FP32 lanes x %d SMs x %.0f MHz (max SM clock of "
                                    "MEASURED_PEAKS.json); no measured FP32 peak exists" % (sms, sm_max)}
     line = {
@@ -283,7 +312,9 @@ def run_ours(a, rank, world, local_rank):
                    "numerics": a.numerics, "samples_per_step": samples_per_step,
                    "l2": "inputs larger than L2 (G-buffer %.0f MB > 129 MB)" % (hs.gbuffer.nbytes / 1e6),
                    "parallelism": "one frame per GPU" if world > 1 else "single GPU"},
-        "gpu_launches": a.steps,
+        "gpu_launches": 2 * a.steps,
+        "kernels": kernels,
+        "exact_numerics_value": exact_value,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,

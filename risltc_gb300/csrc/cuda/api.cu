@@ -7,12 +7,9 @@
 #include "ris_kernels.cuh"
 
 namespace risltc {
-cudaError_t launch_shade_exact(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
-cudaError_t launch_shade_fast(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
+cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast);
 cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,
                                cudaStream_t stream, int grid);
-cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
-cudaError_t launch_ris_fast(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
 }  // namespace risltc
 
 struct risltc_ctx_s {
@@ -294,11 +291,9 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		r.accum = accum;
 		r.reservoirs = reservoirs;
 		r.error = ctx->d_error;
-		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_ris_fast(r, ctx->stream, grid, events)
-		                                                 : risltc::launch_ris_exact(r, ctx->stream, grid, events);
+		e = risltc::launch_ris(r, ctx->stream, grid, events, settings->numerics == risltc_numerics_fast);
 	} else {
-		e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_shade_fast(p, ctx->stream, grid, events)
-		                                                 : risltc::launch_shade_exact(p, ctx->stream, grid, events);
+		e = risltc::launch_shade(p, ctx->stream, grid, events, settings->numerics == risltc_numerics_fast);
 	}
 	if (e != cudaSuccess) return cuda_status(e);
 	noise->random_seed += frame_count;

@@ -16,10 +16,6 @@
 
 risltc::SceneView risltc_scene_view(const risltc_scene_t* scene);
 
-namespace risltc {
-cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
-cudaError_t launch_ris_fast(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events);
-}  // namespace risltc
 
 // The scratch: reservoir records for up to RISLTC_NOALLOC_MAX_PIXEL_FRAMES
 // pixel-frames, then one error word.  Every GPU that loads the library holds
@@ -103,8 +99,7 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 	size_t blocks = ((size_t) gbuffer->width * gbuffer->height + 127) / 128;
 	if (blocks > (size_t) sms * 16) blocks = (size_t) sms * 16;
-	e = (settings->numerics == risltc_numerics_fast) ? risltc::launch_ris_fast(r, s, (int) blocks, nullptr)
-	                                                 : risltc::launch_ris_exact(r, s, (int) blocks, nullptr);
+	e = risltc::launch_ris(r, s, (int) blocks, nullptr, settings->numerics == risltc_numerics_fast);
 	if (e != cudaSuccess) return to_status(e);
 	uint32_t bits = 0;
 	e = cudaMemcpyAsync(&bits, &scratch->error, sizeof(bits), cudaMemcpyDeviceToHost, s);

@@ -278,4 +278,20 @@ template <class P> __global__ void __launch_bounds__(128) ris_shade_kernel(RisPa
 	}
 }
 
+cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid);
+
+// The candidate kernel (fast or exact numerics) then the shading kernel
+// (always exact); events (may be null) are recorded before, between and after.
+inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast) {
+	if (events) cudaEventRecord(events[0], stream);
+	cudaError_t e = fast ? launch_candidates_fast(p, stream, grid) : launch_candidates_exact(p, stream, grid);
+	if (e != cudaSuccess) return e;
+	if (events) cudaEventRecord(events[1], stream);
+	e = launch_ris_shade(p, stream, grid);
+	if (events) cudaEventRecord(events[2], stream);
+	return e;
+}
+
 }  // namespace risltc

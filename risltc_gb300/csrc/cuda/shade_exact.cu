@@ -1,11 +1,16 @@
-// Exact numerics instantiation: compiled with --fmad=false and IEEE division
-// and square root, so every operation matches the CPU restatement bit for bit.
+// Instantiations compiled with --fmad=false and IEEE division and square
+// root: everything that must match the CPU restatement bit for bit, plus the
+// fused kernel's fast-candidate variant (its candidate loop uses hardware
+// reciprocal square root; its final shading stays exact).
 #include "ris_kernels.cuh"
 
 namespace risltc {
-cudaError_t launch_shade_exact(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events) {
+cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast) {
 	if (events) cudaEventRecord(events[0], stream);
-	shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	if (fast)
+		shade_kernel<FastNumerics, ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	else
+		shade_kernel<ExactNumerics, ExactNumerics><<<grid, 128, 0, stream>>>(p);
 	cudaError_t e = cudaGetLastError();
 	if (events) {
 		cudaEventRecord(events[1], stream);
@@ -13,21 +18,17 @@ cudaError_t launch_shade_exact(const ShadeParams& p, cudaStream_t stream, int gr
 	}
 	return e;
 }
+cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid) {
+	ris_candidates_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	return cudaGetLastError();
+}
+cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid) {
+	ris_shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	return cudaGetLastError();
+}
 cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,
                                cudaStream_t stream, int grid) {
 	trace_shadow_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(s, rays, count, hits, error);
 	return cudaGetLastError();
-}
-// events (may be null): recorded before, between and after the two kernels.
-cudaError_t launch_ris_exact(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events) {
-	if (events) cudaEventRecord(events[0], stream);
-	ris_candidates_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
-	cudaError_t e = cudaGetLastError();
-	if (e != cudaSuccess) return e;
-	if (events) cudaEventRecord(events[1], stream);
-	ris_shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
-	e = cudaGetLastError();
-	if (events) cudaEventRecord(events[2], stream);
-	return e;
 }
 }  // namespace risltc

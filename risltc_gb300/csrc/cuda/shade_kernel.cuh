@@ -222,7 +222,8 @@ RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, c
 }
 
 // Body of shading_pass.frag.glsl:main (:674-770) for one pixel and frame.
-template <class P>
+// C is the numerics of the RIS candidate evaluation, P of everything else.
+template <class C, class P>
 RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& ltc, uint32_t seed, bool first_frame,
                       risltc_reservoir_t* res_out) {
 	const int n = pr.scene.light_count;
@@ -256,13 +257,13 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 				idx = idx > n - 1 ? n - 1 : idx;
 				Light l;
 				load_light(pr.scene, idx, l);
-				f3 color = peters ? ltc_cp_target<P>(sd, ltc, l) : psa_mis_shade<P>(pr, sd, ltc, l, seed, false, false);
-				float p_hat = P::sqrt(dot(color, color));
-				float w = P::div(p_hat, p);
+				f3 color = peters ? ltc_cp_target<C>(sd, ltc, l) : psa_mis_shade<C>(pr, sd, ltc, l, seed, false, false);
+				float p_hat = C::sqrt(dot(color, color));
+				float w = C::div(p_hat, p);
 				// insert_in_reservoir, reservoir.glsl:34-41
 				float rnd = get_noise_1(seed);
 				w_sum += w;
-				if (w > 0.0f && rnd < P::div(w, w_sum)) {
+				if (w > 0.0f && rnd < C::div(w, w_sum)) {
 					res_index = idx;
 					sample_value = p_hat;
 				}
@@ -291,7 +292,7 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 	return final_color;
 }
 
-template <class P> __global__ void __launch_bounds__(128) shade_kernel(ShadeParams pr) {
+template <class C, class P> __global__ void __launch_bounds__(128) shade_kernel(ShadeParams pr) {
 	const uint32_t np = pr.width * pr.height;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
 		const uint32_t x = i % pr.width, y = i / pr.width;
@@ -321,7 +322,7 @@ template <class P> __global__ void __launch_bounds__(128) shade_kernel(ShadePara
 		for (uint32_t f = 0; f != pr.frame_count; ++f) {
 			uint32_t rn_x = pr.animate ? wang_random_number((pr.noise_seed + f) * 4u) : 0u;
 			uint32_t seed = get_noise_accessor(x, y, pr.width, rn_x);
-			f3 c = shade_pixel<P>(pr, sd, ltc, seed, f == 0, res);
+			f3 c = shade_pixel<C, P>(pr, sd, ltc, seed, f == 0, res);
 			sum = add(sum, c);
 			acc[0] += (double) c.x;
 			acc[1] += (double) c.y;

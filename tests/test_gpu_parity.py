@@ -15,11 +15,13 @@ import oracle
 
 pytestmark = pytest.mark.gpu
 
-# Fast-numerics tolerance against the FP32 oracle (hardware reciprocal square
-# root and approximate division): relative error of the pixel estimate.
-FAST_MEDIAN_REL = 1e-5
-FAST_P99_REL = 1e-2
-FAST_INDEX_AGREEMENT = 0.99
+# Fast numerics (hardware reciprocal square root and approximate division in
+# the RIS candidate loop only) against the FP32 oracle: where both choose the
+# same light, the pixel estimate is within 1e-5 relative (the north-star
+# tolerance) for 99% of pixels; the light choice itself agrees on 99.9%.
+FAST_REL = 1e-5
+FAST_REL_QUANTILE = 0.99
+FAST_INDEX_AGREEMENT = 0.999
 
 
 @pytest.fixture(scope="module")
@@ -128,9 +130,10 @@ def test_fast_numerics_within_tolerance(rl):
     orgb, ores, _ = oracle_render(sc, c, c["random_numbers"][0])
     agree = idx == ores["light_index"]
     assert agree.mean() >= FAST_INDEX_AGREEMENT
-    rel = np.abs(rgb[agree] - orgb[agree]) / np.maximum(np.abs(orgb[agree]), 1e-6)
-    assert np.median(rel) <= FAST_MEDIAN_REL
-    assert np.quantile(rel, 0.99) <= FAST_P99_REL
+    lum_g, lum_o = rgb.sum(1), orgb.sum(1)
+    m = agree & (lum_o > 0)
+    rel = np.abs(lum_g[m] - lum_o[m]) / lum_o[m]
+    assert np.quantile(rel, FAST_REL_QUANTILE) <= FAST_REL
 
 
 def test_host_entry_point_equals_device_entry_point(rl):
