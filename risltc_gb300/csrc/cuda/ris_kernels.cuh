@@ -50,7 +50,7 @@ struct RisParams {
 template <class P> RL_DEV float ltc_integral_unclipped(const f3 (&v)[kMaxLightVertices], uint32_t n) {
 	f3 nv[kMaxLightVertices];
 #pragma unroll
-	for (int i = 0; i != kMaxLightVertices; ++i) nv[i] = normalize<P>(v[i]);
+	for (int i = 0; i != kMaxLightVertices; ++i) nv[i] = (i < (int) n) ? normalize<P>(v[i]) : v[i];
 	f3 last = nv[2];
 #pragma unroll
 	for (int j = 3; j != kMaxLightVertices; ++j)
