@@ -1,0 +1,287 @@
+// ris_binned.cuh - the RIS candidate phase as a warp-per-tile kernel with
+// work binning.
+//
+// Each warp owns 32 consecutive pixels.  Per chunk of kChunk candidates the
+// warp
+//   1. draws every pixel's candidate lights from that pixel's noise stream
+//      (the LCG sequence of shading_pass.frag.glsl:728-736: a light draw, then
+//      the reservoir draw, per candidate);
+//   2. sorts the chunk's (pixel, candidate) items by the light's vertex count
+//      with a counting sort over the warp, so that the lanes of one step
+//      mostly evaluate polygons with the same number of vertices;
+//   3. evaluates the items with each pixel's LTC frame read from shared
+//      memory; an item whose polygon is partially clipped in either space is
+//      deferred, and the warp evaluates the deferred items together;
+//   4. lets each lane replay its pixel's reservoir updates in candidate order
+//      (insert_in_reservoir, reservoir.glsl:34-41).
+// Every p_hat is computed by the same operations on the same values as in
+// ris_candidates_kernel and the reservoir sees them in the same order, so the
+// reservoir records are bit-identical.
+#pragma once
+#include "ris_kernels.cuh"
+
+namespace risltc {
+
+#ifndef RISLTC_CANDIDATES_BINNED
+#define RISLTC_CANDIDATES_BINNED 1
+#endif
+#ifndef RISLTC_BINNED_CHUNK
+#define RISLTC_BINNED_CHUNK 8
+#endif
+#ifndef RISLTC_BINNED_MIN_BLOCKS
+#define RISLTC_BINNED_MIN_BLOCKS 5
+#endif
+constexpr int kChunk = RISLTC_BINNED_CHUNK;  // candidates per pixel per chunk
+constexpr int kItems = 32 * kChunk;          // items per warp per chunk
+constexpr int kFrameWords = 45;              // 44 used; odd stride avoids bank conflicts
+constexpr int kBinnedWarps = 4;              // warps per block
+constexpr int kBins = kMaxLightVertices - 2; // vertex counts 3..8
+static_assert(kItems < 1024, "10-bit bin counters");
+
+struct WarpTile {
+	float frame[32][kFrameWords];
+	int32_t item_light[kItems];
+	uint16_t item_slot[kItems];  // pixel lane * kChunk + candidate of the chunk
+	uint16_t deferred[kItems];
+	float p_hat[kItems];         // [pixel lane][candidate of the chunk]
+	uint32_t deferred_count;
+};
+
+// Frame layout: position (0-2), diffuse albedo (3-5), LTC albedo (6),
+// world to shading (7-18), world to cosine (19-30) and its y-flipped
+// counterpart (31-42); each mat4x3 column-major.
+RL_DEV void store_frame(float* f, const CandidateFrame& cf) {
+	f[0] = cf.position.x;
+	f[1] = cf.position.y;
+	f[2] = cf.position.z;
+	f[3] = cf.diffuse_albedo.x;
+	f[4] = cf.diffuse_albedo.y;
+	f[5] = cf.diffuse_albedo.z;
+	f[6] = cf.ltc_albedo;
+#pragma unroll
+	for (int c = 0; c != 4; ++c) {
+		f[7 + 3 * c + 0] = cf.w2s.c[c].x;
+		f[7 + 3 * c + 1] = cf.w2s.c[c].y;
+		f[7 + 3 * c + 2] = cf.w2s.c[c].z;
+		f[19 + 3 * c + 0] = cf.w2c[0].c[c].x;
+		f[19 + 3 * c + 1] = cf.w2c[0].c[c].y;
+		f[19 + 3 * c + 2] = cf.w2c[0].c[c].z;
+		f[31 + 3 * c + 0] = cf.w2c[1].c[c].x;
+		f[31 + 3 * c + 1] = cf.w2c[1].c[c].y;
+		f[31 + 3 * c + 2] = cf.w2c[1].c[c].z;
+	}
+}
+
+// One candidate (ltc_cp_candidate, then p_hat = length(color)) with the
+// frame in shared memory.  The two LTC integrals run in one loop over the
+// spaces to keep the code small.  With allow_clip false, returns false as
+// soon as a space clips the polygon partially; the caller defers the item.
+template <class P>
+RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+	const float4 head = __ldg(record), pl = __ldg(record + 1);
+	const uint32_t n = __float_as_uint(head.w);
+	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
+	const bool flip = plane_dot(mk3(f[0], f[1], f[2]), plane) < 0.0f;
+	float integral[2];
+	bool away[2];
+#pragma unroll 1
+	for (int s = 0; s != 2; ++s) {
+		const float* m = f + (s == 0 ? 7 : (flip ? 31 : 19));
+		mat43 t;
+#pragma unroll
+		for (int c = 0; c != 4; ++c) t.c[c] = mk3(m[3 * c], m[3 * c + 1], m[3 * c + 2]);
+		const bool negate_y = s == 0 && flip;
+		PolygonVerts v;
+		uint32_t above = 0;
+#pragma unroll
+		for (int j = 0; j != kMaxLightVertices; ++j) {
+			const float4 q = __ldg(record + 2 + j);
+			v.v[j] = mul_point(t, mk3(q.x, q.y, q.z));
+			v.v[j].y = negate_y ? -v.v[j].y : v.v[j].y;
+			if (j < (int) n && v.v[j].z > 0.0f) ++above;
+		}
+		const bool partial = above != 0 && above != n;
+		if (partial && !allow_clip) return false;
+		float r = 0.0f;
+		bool a = above == 0;
+		if (above == n) {
+			r = ltc_integral_unclipped<P>(v.v, n);
+		} else if (partial) {
+			r = ltc_integral_clipped<P>(v, n);
+			a = r < 0.0f;
+			r = a ? 0.0f : r;
+		}
+		if (s == 0) {
+			integral[0] = r;
+			away[0] = a;
+		} else {
+			integral[1] = r;
+			away[1] = a;
+		}
+	}
+	const f3 radiance = mk3(head.x, head.y, head.z);
+	f3 result = splat(0.0f);
+	const f3 diffuse = away[0] ? splat(0.0f) : mul(scale(mk3(f[3], f[4], f[5]), integral[0]), radiance);
+	result = add(result, diffuse);
+	const f3 ggx = away[1] ? splat(0.0f) : mul(splat(integral[1] * f[6]), radiance);
+	const f3 color = add(result, ggx);
+	p_hat = P::sqrt(dot(color, color));
+	return true;
+}
+
+template <class P>
+__global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
+ris_candidates_binned_kernel(RisParams pr) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	WarpTile& tile = reinterpret_cast<WarpTile*>(smem_raw)[threadIdx.x / 32];
+	const uint32_t lane = threadIdx.x % 32;
+	const uint32_t np = pr.width * pr.height;
+	const int n_lights = pr.scene.light_count;
+	const float p = P::rcp((float) n_lights);
+	const uint32_t warps_total = gridDim.x * kBinnedWarps;
+	const uint32_t tiles = (np + 31) / 32;
+	for (uint32_t t = blockIdx.x * kBinnedWarps + threadIdx.x / 32; t < tiles; t += warps_total) {
+		const uint32_t i = t * 32 + lane;
+		const bool valid = i < np && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
+		if (valid) {
+			const float* g = pr.gbuffer;
+			const size_t snp = np;
+			const f3 position = mk3(g[0 * snp + i], g[1 * snp + i], g[2 * snp + i]);
+			const f3 normal = mk3(g[3 * snp + i], g[4 * snp + i], g[5 * snp + i]);
+			const f3 outgoing = mk3(g[6 * snp + i], g[7 * snp + i], g[8 * snp + i]);
+			const f3 fresnel_0 = mk3(g[13 * snp + i], g[14 * snp + i], g[15 * snp + i]);
+			const float roughness = g[16 * snp + i];
+			CandidateFrame cf;
+			cf.position = position;
+			cf.diffuse_albedo = mk3(g[10 * snp + i], g[11 * snp + i], g[12 * snp + i]);
+			const float fl = dot(fresnel_0, mk3(0.2126f, 0.7152f, 0.0722f));
+			const Ltc ltc = get_ltc_coefficients<P>(pr.scene, fl, roughness, position, normal, outgoing);
+			cf.ltc_albedo = ltc.albedo;
+			cf.w2s = ltc.world_to_shading;
+			mat43 flipped = ltc.world_to_shading;
+#pragma unroll
+			for (int c = 0; c != 4; ++c) flipped.c[c].y = -flipped.c[c].y;
+			cf.w2c[0] = mul(ltc.shading_to_cosine, cf.w2s);
+			cf.w2c[1] = mul(ltc.shading_to_cosine, flipped);
+			store_frame(tile.frame[lane], cf);
+		}
+		__syncwarp();
+		const uint32_t x = i % pr.width, y = i / pr.width;
+		for (uint32_t f = 0; f != pr.frame_count; ++f) {
+			uint32_t seed = 0;
+			if (valid) {
+				const uint32_t rn_x = pr.animate ? wang_random_number((pr.noise_seed + f) * 4u) : 0u;
+				seed = get_noise_accessor(x, y, pr.width, rn_x);
+			}
+			float w_sum = 0.0f, sample_value = 0.0f;
+			int res_index = -1;
+			for (int c0 = 0; c0 < pr.candidate_count; c0 += kChunk) {
+				const int chunk = min(kChunk, pr.candidate_count - c0);
+				// 1. This lane's candidate lights; bin them by vertex count
+				//    (six 10-bit counters).
+				int light[kChunk];
+				uint32_t bin[kChunk];
+				uint32_t draw = seed;
+				unsigned long long counts = 0;
+#pragma unroll
+				for (int k = 0; k != kChunk; ++k) {
+					light[k] = -1;
+					bin[k] = kBins;
+					if (valid && k < chunk) {
+						int idx = (int) (get_noise_1(draw) * (float) n_lights);
+						idx = idx > n_lights - 1 ? n_lights - 1 : idx;
+						get_noise_1(draw);
+						light[k] = idx;
+						bin[k] = __float_as_uint(__ldg(light_record(pr.scene, idx)).w) - 3u;
+						counts += 1ull << (10 * bin[k]);
+					}
+				}
+				// 2. Counting sort: exclusive scan of the counters across the
+				//    warp, then each bin's start.
+				unsigned long long prefix = counts;
+#pragma unroll
+				for (int d = 1; d < 32; d <<= 1) {
+					const unsigned long long o = __shfl_up_sync(0xffffffffu, prefix, d);
+					if ((int) lane >= d) prefix += o;
+				}
+				const unsigned long long totals = __shfl_sync(0xffffffffu, prefix, 31);
+				prefix -= counts;
+				uint32_t start[kBins + 1];
+				start[0] = 0;
+#pragma unroll
+				for (int b = 0; b != kBins; ++b) start[b + 1] = start[b] + (uint32_t) ((totals >> (10 * b)) & 1023u);
+				const uint32_t item_count = start[kBins];
+#pragma unroll
+				for (int k = 0; k != kChunk; ++k) {
+					if (bin[k] < kBins) {
+						const uint32_t b = bin[k];
+						uint32_t s = 0;
+#pragma unroll
+						for (int q = 0; q != kBins; ++q)
+							if (q == (int) b) s = start[q];
+						const uint32_t pos = s + (uint32_t) ((prefix >> (10 * b)) & 1023u);
+						prefix += 1ull << (10 * b);
+						tile.item_light[pos] = light[k];
+						tile.item_slot[pos] = (uint16_t) (lane * kChunk + k);
+					}
+				}
+				if (lane == 0) tile.deferred_count = 0;
+				__syncwarp();
+				// 3. Evaluate the sorted items, 32 at a time; defer partial clips.
+				for (uint32_t base = 0; base < item_count; base += 32) {
+					const uint32_t it = base + lane;
+					if (it < item_count) {
+						const uint32_t slot = tile.item_slot[it];
+						float ph;
+						if (binned_candidate<P>(tile.frame[slot / kChunk], light_record(pr.scene, tile.item_light[it]),
+						                        false, ph))
+							tile.p_hat[slot] = ph;
+						else
+							tile.deferred[atomicAdd(&tile.deferred_count, 1u)] = (uint16_t) it;
+					}
+				}
+				__syncwarp();
+				const uint32_t deferred = tile.deferred_count;
+				for (uint32_t base = 0; base < deferred; base += 32) {
+					const uint32_t d = base + lane;
+					if (d < deferred) {
+						const uint32_t it = tile.deferred[d];
+						const uint32_t slot = tile.item_slot[it];
+						float ph = 0.0f;
+						binned_candidate<P>(tile.frame[slot / kChunk], light_record(pr.scene, tile.item_light[it]), true,
+						                    ph);
+						tile.p_hat[slot] = ph;
+					}
+				}
+				__syncwarp();
+				// 4. Reservoir updates in candidate order.
+				if (valid) {
+#pragma unroll
+					for (int k = 0; k != kChunk; ++k) {
+						if (k < chunk) {
+							get_noise_1(seed);
+							const float rnd = get_noise_1(seed);
+							const float p_hat = tile.p_hat[lane * kChunk + k];
+							const float w = P::div(p_hat, p);
+							w_sum += w;
+							if (w > 0.0f && rnd < P::div(w, w_sum)) {
+								res_index = light[k];
+								sample_value = p_hat;
+							}
+						}
+					}
+				}
+				__syncwarp();
+			}
+			if (valid)
+				pr.records[(size_t) f * np + i] = ReservoirRecord{res_index, w_sum, sample_value, seed};
+			else if (i < np)
+				pr.records[(size_t) f * np + i] = ReservoirRecord{-1, 0.0f, 0.0f, 0u};
+		}
+		__syncwarp();
+	}
+}
+
+inline constexpr size_t binned_smem_bytes() { return sizeof(WarpTile) * kBinnedWarps; }
+
+}  // namespace risltc

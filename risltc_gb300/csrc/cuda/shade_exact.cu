@@ -2,7 +2,7 @@
 // root: everything that must match the CPU restatement bit for bit, plus the
 // fused kernel's fast-candidate variant (its candidate loop uses hardware
 // reciprocal square root; its final shading stays exact).
-#include "ris_kernels.cuh"
+#include "ris_binned.cuh"
 
 namespace risltc {
 cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast) {
@@ -19,7 +19,11 @@ cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cu
 	return e;
 }
 cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid) {
+#if RISLTC_CANDIDATES_BINNED
+	ris_candidates_binned_kernel<ExactNumerics><<<grid, 32 * kBinnedWarps, binned_smem_bytes(), stream>>>(p);
+#else
 	ris_candidates_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+#endif
 	return cudaGetLastError();
 }
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid) {

@@ -1,11 +1,15 @@
 // Fast-numerics candidate kernel: hardware reciprocal square root,
 // approximate division and contraction of multiply-add (--fmad=true) in the
 // RIS candidate loop, whose results only weight the reservoir.
-#include "ris_kernels.cuh"
+#include "ris_binned.cuh"
 
 namespace risltc {
 cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid) {
+#if RISLTC_CANDIDATES_BINNED
+	ris_candidates_binned_kernel<FastNumerics><<<grid, 32 * kBinnedWarps, binned_smem_bytes(), stream>>>(p);
+#else
 	ris_candidates_kernel<FastNumerics><<<grid, 128, 0, stream>>>(p);
+#endif
 	return cudaGetLastError();
 }
 }  // namespace risltc
