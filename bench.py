@@ -145,12 +145,17 @@ def cpu_sample(hs, a, seconds_target, threads=0, seed=1, count_ops=True, repeats
         # Counted with M and with one candidate: the difference is the
         # candidate phase, the rest the final PSA/MIS shading.
         ops_g, m = _pixel_subset(hs, 1024, seed + 2)
+        # Counted once more without occluders: the difference is the
+        # shadow rays' BVH traversal.
         ops = oracle.opcount(osc, st, ops_g, m, 1, rn, (0, 1))
         one = oracle.opcount(osc, oracle.make_settings(candidates=1), ops_g, m, 1, rn, (0, 1))
+        unshadowed = oracle.OracleScene(hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants)
+        lit = oracle.opcount(unshadowed, st, ops_g, m, 1, rn, (0, 1))
         per_candidate = (ops["flops"] - one["flops"]) / m / max(a.candidates - 1, 1)
         out["flops_per_sample"] = ops["flops"] / m
         out["candidate_flops_per_sample"] = per_candidate * a.candidates
-        out["shade_flops_per_sample"] = ops["flops"] / m - per_candidate * a.candidates
+        out["shade_flops_per_sample"] = lit["flops"] / m - per_candidate * a.candidates
+        out["trace_flops_per_sample"] = (ops["flops"] - lit["flops"]) / m
         out["ops"] = {k: v for k, v in ops.items() if k != "rgb"}
     return out
 
@@ -219,7 +224,7 @@ def run_ours(a, rank, world, local_rank):
     if dist:
         dist.barrier()
     clock_info = clocks.stop() if clocks else None
-    cand_ms, shade_ms, timed_calls = ctx.profile(False)
+    prof = ctx.profile(False)
     ctx.check()
     # The same step with the other numerics mode, for reference (exact is
     # bit-identical to the oracle; fast approximates the candidate loop).
@@ -288,13 +293,21 @@ def run_ours(a, rank, world, local_rank):
                "kind": "port", "sample": "%d pixel-samples drawn uniformly from the same frame at 1 spp, FP32 "
                                          "oracle (C99, OpenMP over rows of 256)" % info["samples"]}
     roofline = None
-    kernels = {"ris_candidates_kernel": {"ms_per_launch": cand_ms / max(timed_calls, 1)},
-               "ris_shade_kernel": {"ms_per_launch": shade_ms / max(timed_calls, 1)}}
+    calls = max(prof["calls"], 1)
+    # One launch of each kernel per step (all spp frames in one call).  The
+    # resolve kernel's few operations are counted with the sample kernel.
+    kernels = {"ris_candidates_kernel": {"ms_per_launch": prof["candidates"] / calls},
+               "ris_sample_kernel": {"ms_per_launch": prof["shade"] / calls},
+               "shadow_trace_kernel": {"ms_per_launch": prof["shadow_trace"] / calls},
+               "ris_resolve_kernel": {"ms_per_launch": prof["resolve"] / calls}}
     if flops_per_sample:
         kernels["ris_candidates_kernel"]["flops_per_sample"] = info["candidate_flops_per_sample"]
-        kernels["ris_shade_kernel"]["flops_per_sample"] = info["shade_flops_per_sample"]
+        kernels["ris_sample_kernel"]["flops_per_sample"] = info["shade_flops_per_sample"]
+        kernels["shadow_trace_kernel"]["flops_per_sample"] = info["trace_flops_per_sample"]
+        kernels["ris_resolve_kernel"]["flops_per_sample"] = 0.0
         for k in kernels.values():
-            k["achieved_tflops"] = k["flops_per_sample"] * samples_per_step / (k["ms_per_launch"] / 1e3) / 1e12
+            k["achieved_tflops"] = (k["flops_per_sample"] * samples_per_step / (k["ms_per_launch"] / 1e3) / 1e12
+                                    if k["ms_per_launch"] > 0 else 0.0)
             k["frac"] = k["achieved_tflops"] / fp32_peak
         dominant = max(kernels, key=lambda k: kernels[k]["ms_per_launch"])
         d = kernels[dominant]
@@ -313,7 +326,7 @@ def run_ours(a, rank, world, local_rank):
                    "numerics": a.numerics, "samples_per_step": samples_per_step,
                    "l2": "inputs larger than L2 (G-buffer %.0f MB > 129 MB)" % (hs.gbuffer.nbytes / 1e6),
                    "parallelism": "one frame per GPU" if world > 1 else "single GPU"},
-        "gpu_launches": 2 * a.steps,
+        "gpu_launches": 4 * a.steps,
         "kernels": kernels,
         "other_numerics": {"numerics": other, "value": other_value, "unit": "Gsamples/s"},
         "roofline": roofline,

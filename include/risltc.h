@@ -341,11 +341,14 @@ EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene,
 
 /* Kernel timing with CUDA events on the context's stream.  Returns the time
  * of the shading calls made since the previous call of this function (at
- * most 64 calls are timed), split into phase_ms[0] (the RIS candidate kernel,
- * or the fused kernel) and phase_ms[1] (the shading kernel; 0 for the fused
- * kernel), and their number in calls; then enables (enable != 0) or disables
- * timing of the following calls.  phase_ms and calls may be NULL.  Querying
- * synchronises the stream. */
+ * most 64 calls are timed), split into RISLTC_PROFILE_PHASES phases:
+ * phase_ms[0] the RIS candidate kernel (or the fused kernel), phase_ms[1] the
+ * shading kernel (with its shadow rays, or up to queueing them), phase_ms[2]
+ * the shadow-ray kernel and phase_ms[3] the resolve kernel (0 where a phase
+ * is not a kernel of its own), and their number in calls; then enables
+ * (enable != 0) or disables timing of the following calls.  phase_ms and
+ * calls may be NULL.  Querying synchronises the stream. */
+#define RISLTC_PROFILE_PHASES 4
 EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, uint32_t* calls);
 
 /* Synchronises the context's stream and returns the first error recorded by

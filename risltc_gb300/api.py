@@ -73,12 +73,14 @@ class Context:
 
     def profile(self, enable=True):
         """Per-kernel CUDA-event times (ms) of the shading calls since the last
-        call: (candidate or fused kernel, shading kernel, number of calls);
-        then switches timing on or off."""
-        ms = (ctypes.c_float * 2)()
+        call, then switches timing on or off.  Returns a dict: candidates
+        (or the fused kernel), shade, shadow_trace and resolve (0 where the
+        phase is not a kernel of its own), and calls."""
+        ms = (ctypes.c_float * 4)()
         calls = ctypes.c_uint32(0)
         check(self._lib.risltc_ctx_profile(self._h, int(enable), ms, ctypes.byref(calls)), "risltc_ctx_profile")
-        return float(ms[0]), float(ms[1]), int(calls.value)
+        return dict(candidates=float(ms[0]), shade=float(ms[1]), shadow_trace=float(ms[2]), resolve=float(ms[3]),
+                    calls=int(calls.value))
 
     def close(self):
         if self._h:

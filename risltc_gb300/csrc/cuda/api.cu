@@ -4,7 +4,7 @@
 #include <cstring>
 #include <vector>
 #include <cuda_runtime.h>
-#include "ris_kernels.cuh"
+#include "ris_wavefront.cuh"
 
 namespace risltc {
 cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast);
@@ -26,11 +26,19 @@ struct risltc_ctx_s {
 	// Reservoir records between the candidate and shading kernels.
 	risltc::ReservoirRecord* d_records;
 	size_t record_capacity;
-	// Kernel timing: three events per shading call (before, between and
-	// after the two phases), up to kTimedCalls calls between queries.
+	// The shading phase's state between its sample, shadow-trace and resolve
+	// kernels: a 64-byte sample record per pixel-frame, a queue of up to two
+	// 32-byte shadow rays per pixel-frame, their outcomes and the queue length.
+	risltc::SampleRecord* d_samples;
+	risltc::ShadowRay* d_rays;
+	uint8_t* d_hits;
+	uint32_t* d_ray_count;
+	size_t wavefront_capacity;
+	// Kernel timing: five events per shading call (before, between and after
+	// the phases), up to 64 calls between queries.
 	int profiling;
 	int timed_calls;
-	cudaEvent_t events[64][3];
+	cudaEvent_t events[64][5];
 	int events_created;
 };
 
@@ -60,6 +68,26 @@ int grid_for(const risltc_ctx_t* ctx, size_t items) {
 	size_t cap = (size_t) ctx->sm_count * 16;
 	if (blocks > cap) blocks = cap;
 	return (int) (blocks ? blocks : 1);
+}
+
+int reserve_wavefront(risltc_ctx_t* ctx, size_t pixel_frames) {
+	if (pixel_frames <= ctx->wavefront_capacity) return RISLTC_OK;
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_samples);
+	cudaFree(ctx->d_rays);
+	cudaFree(ctx->d_hits);
+	ctx->d_samples = nullptr;
+	ctx->d_rays = nullptr;
+	ctx->d_hits = nullptr;
+	ctx->wavefront_capacity = 0;
+	cudaError_t e = cudaSuccess;
+	if (!ctx->d_ray_count) e = cudaMalloc(&ctx->d_ray_count, sizeof(uint32_t));
+	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_samples, pixel_frames * sizeof(risltc::SampleRecord));
+	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rays, 2 * pixel_frames * sizeof(risltc::ShadowRay));
+	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_hits, 2 * pixel_frames);
+	if (e != cudaSuccess) return cuda_status(e);
+	ctx->wavefront_capacity = pixel_frames;
+	return RISLTC_OK;
 }
 
 }  // namespace
@@ -97,8 +125,12 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFree(ctx->d_rgb);
 	cudaFreeHost(ctx->h_pinned_rgb);
 	cudaFree(ctx->d_records);
+	cudaFree(ctx->d_samples);
+	cudaFree(ctx->d_rays);
+	cudaFree(ctx->d_hits);
+	cudaFree(ctx->d_ray_count);
 	for (int i = 0; i < ctx->events_created; ++i)
-		for (int k = 0; k != 3; ++k) cudaEventDestroy(ctx->events[i][k]);
+		for (int k = 0; k != 5; ++k) cudaEventDestroy(ctx->events[i][k]);
 	free(ctx);
 }
 
@@ -259,7 +291,7 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 	if (ctx->profiling && ctx->timed_calls < 64) {
 		int i = ctx->timed_calls++;
 		if (i >= ctx->events_created) {
-			for (int k = 0; k != 3; ++k) cudaEventCreate(&ctx->events[i][k]);
+			for (int k = 0; k != 5; ++k) cudaEventCreate(&ctx->events[i][k]);
 			ctx->events_created = i + 1;
 		}
 		events = ctx->events[i];
@@ -287,11 +319,24 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		r.animate = p.animate;
 		r.frame_count = p.frame_count;
 		r.records = ctx->d_records;
+		// Shadow rays in their own pass for one sample per technique; the
+		// queue's hit slots (2 per pixel-frame) are 32-bit.
+		const size_t pixel_frames = pixels * frame_count;
+		if (settings->shadows && scene->view.triangle_count && settings->sample_count == 1 &&
+		    pixel_frames < (1ull << 31)) {
+			st = reserve_wavefront(ctx, pixel_frames);
+			if (st) return st;
+			r.samples = ctx->d_samples;
+			r.rays = ctx->d_rays;
+			r.ray_count = ctx->d_ray_count;
+			r.hits = ctx->d_hits;
+		}
 		r.out_rgb = out_rgb;
 		r.accum = accum;
 		r.reservoirs = reservoirs;
 		r.error = ctx->d_error;
-		e = risltc::launch_ris(r, ctx->stream, grid, events, settings->numerics == risltc_numerics_fast);
+		e = risltc::launch_ris(r, ctx->stream, grid, grid_for(ctx, 2 * pixels * frame_count), events,
+		                       settings->numerics == risltc_numerics_fast);
 	} else {
 		e = risltc::launch_shade(p, ctx->stream, grid, events, settings->numerics == risltc_numerics_fast);
 	}
@@ -370,16 +415,16 @@ EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, 
 	cudaSetDevice(ctx->device);
 	int status = RISLTC_OK;
 	if (phase_ms) {
-		phase_ms[0] = phase_ms[1] = 0.0f;
+		for (int k = 0; k != RISLTC_PROFILE_PHASES; ++k) phase_ms[k] = 0.0f;
 		cudaError_t e = cudaStreamSynchronize(ctx->stream);
 		if (e != cudaSuccess) return cuda_status(e);
 		for (int i = 0; i != ctx->timed_calls; ++i) {
-			float a = 0.0f, b = 0.0f;
-			if (cudaEventElapsedTime(&a, ctx->events[i][0], ctx->events[i][1]) != cudaSuccess ||
-			    cudaEventElapsedTime(&b, ctx->events[i][1], ctx->events[i][2]) != cudaSuccess)
-				status = RISLTC_ERROR_CUDA;
-			phase_ms[0] += a;
-			phase_ms[1] += b;
+			for (int k = 0; k != RISLTC_PROFILE_PHASES; ++k) {
+				float ms = 0.0f;
+				if (cudaEventElapsedTime(&ms, ctx->events[i][k], ctx->events[i][k + 1]) != cudaSuccess)
+					status = RISLTC_ERROR_CUDA;
+				phase_ms[k] += ms;
+			}
 		}
 	}
 	if (calls) *calls = (uint32_t) ctx->timed_calls;

@@ -99,7 +99,7 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 	size_t blocks = ((size_t) gbuffer->width * gbuffer->height + 127) / 128;
 	if (blocks > (size_t) sms * 16) blocks = (size_t) sms * 16;
-	e = risltc::launch_ris(r, s, (int) blocks, nullptr, settings->numerics == risltc_numerics_fast);
+	e = risltc::launch_ris(r, s, (int) blocks, (int) blocks, nullptr, settings->numerics == risltc_numerics_fast);
 	if (e != cudaSuccess) return to_status(e);
 	uint32_t bits = 0;
 	e = cudaMemcpyAsync(&bits, &scratch->error, sizeof(bits), cudaMemcpyDeviceToHost, s);

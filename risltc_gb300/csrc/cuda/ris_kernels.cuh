@@ -38,6 +38,11 @@ struct RisParams {
 	uint32_t animate;
 	uint32_t frame_count;
 	ReservoirRecord* records;  // [frame][pixel] scratch
+	// Shadow rays traced in their own pass (null: traced in ris_shade_kernel).
+	struct SampleRecord* samples;  // [frame][pixel]
+	struct ShadowRay* rays;        // compacted queue, up to 2 per pixel-frame
+	uint32_t* ray_count;           // queue length (zeroed before the sample pass)
+	uint8_t* hits;                 // [frame][pixel][technique] occlusion
 	float* out_rgb;
 	double* accum;
 	risltc_reservoir_t* reservoirs;
@@ -281,16 +286,36 @@ template <class P> __global__ void __launch_bounds__(128) ris_shade_kernel(RisPa
 cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_ris_sample(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_shadow_trace(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_ris_resolve(const RisParams& p, cudaStream_t stream, int grid);
 
-// The candidate kernel (fast or exact numerics) then the shading kernel
-// (always exact); events (may be null) are recorded before, between and after.
-inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast) {
+// The candidate kernel (fast or exact numerics), then the shading phase
+// (always exact): ris_shade_kernel, or with p.samples set the sample, shadow
+// trace and resolve kernels.  events (may be null) holds five events,
+// recorded before, between and after the phases (the last three together for
+// ris_shade_kernel).
+inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid, int trace_grid, cudaEvent_t* events,
+                              bool fast) {
 	if (events) cudaEventRecord(events[0], stream);
 	cudaError_t e = fast ? launch_candidates_fast(p, stream, grid) : launch_candidates_exact(p, stream, grid);
 	if (e != cudaSuccess) return e;
 	if (events) cudaEventRecord(events[1], stream);
-	e = launch_ris_shade(p, stream, grid);
-	if (events) cudaEventRecord(events[2], stream);
+	if (p.samples) {
+		e = cudaMemsetAsync(p.ray_count, 0, sizeof(uint32_t), stream);
+		if (e == cudaSuccess) e = launch_ris_sample(p, stream, grid);
+		if (e != cudaSuccess) return e;
+		if (events) cudaEventRecord(events[2], stream);
+		e = launch_shadow_trace(p, stream, trace_grid);
+		if (e != cudaSuccess) return e;
+		if (events) cudaEventRecord(events[3], stream);
+		e = launch_ris_resolve(p, stream, grid);
+		if (events) cudaEventRecord(events[4], stream);
+	} else {
+		e = launch_ris_shade(p, stream, grid);
+		if (events)
+			for (int k = 2; k != 5; ++k) cudaEventRecord(events[k], stream);
+	}
 	return e;
 }
 

@@ -1,0 +1,282 @@
+// ris_wavefront.cuh - the shading phase of the two-kernel pipeline with its
+// shadow rays traced in a separate pass:
+//
+//   ris_sample_kernel: per pixel and frame, the estimator of
+//     evaluate_polygonal_light_shading_peters (shading_pass.frag.glsl:292-397)
+//     for the chosen light up to the visibility test.  For each of its (at
+//     most two) samples it stores the MIS-weighted contribution for both
+//     outcomes of the shadow ray and appends the ray to a compacted queue.
+//   shadow_trace_kernel: one any-hit query per queued ray, with a small
+//     register footprint and no divergence from the shading code around it.
+//   ris_resolve_kernel: per pixel, picks each sample's contribution by its
+//     ray's outcome and finishes the frame and the accumulation exactly as
+//     ris_shade_kernel does.
+// The contributions are the same operations on the same values, added in
+// the same order, so the pixels are bit-identical to ris_shade_kernel's.
+// Used for one sample per technique (SAMPLE_COUNT == 1, the reference's
+// default) with shadows on.
+#pragma once
+#include "ris_kernels.cuh"
+
+namespace risltc {
+
+// Per-sample mode, two bits per technique j in SampleRecord::flags.
+enum : uint32_t {
+	kSampleSkip = 0,    // no contribution (dir.z <= 0 or no such sample)
+	kSampleFixed = 1,   // contribution c[j][0], no ray needed
+	kSampleTraced = 2,  // c[j][0] if the ray is unoccluded, else c[j][1]
+	kSampleNoLight = 1u << 8,  // empty reservoir: the frame's colour is zero
+};
+
+// The estimator's state between the sample and resolve kernels (64 bytes).
+struct SampleRecord {
+	float c[2][2][3];  // [technique][unoccluded, occluded][rgb]
+	float W;           // the reservoir's unbiased contribution weight
+	uint32_t flags;
+	uint32_t pad[2];
+};
+static_assert(sizeof(SampleRecord) == 64, "SampleRecord layout");
+
+// A queued shadow ray: origin and the hit slot (2 * pixel-frame + technique),
+// direction and t_max (t_min is get_polygon_visibility's 1e-3).
+struct ShadowRay {
+	float4 origin_slot;
+	float4 dir_tmax;
+};
+
+// evaluate_polygonal_light_shading_peters for SAMPLE_COUNT == 1 up to the
+// visibility test.  Returns the two techniques' modes; fills c and ray.
+template <class P>
+RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l, uint32_t& seed,
+                             f3 (&c)[2][2], ShadowRay (&ray)[2]) {
+	const bool fa = pr.fast_atan != 0;
+	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
+	PsaPolygon pd, ps;
+	if (!psa_prepare_both<P>(pr, sd, ltc, l, pd, ps)) return 0;
+	float specular_weight = ltc.albedo * ps.psa;
+	f3 diffuse_weight = scale(max3(sd.diffuse_albedo, splat(0.01f)), pd.psa);
+	int technique_count = (ps.psa > 0.0f) ? 2 : 1;
+	float rcp_d = P::rcp(pd.psa);
+	float rcp_s = P::rcp(ps.psa);
+	f3 specular_weight_rgb = splat(specular_weight);
+	if (pr.mis_heuristic == mis_heuristic_optimal) {
+		f3 rop = scale(l.radiance, kInvPi);
+		diffuse_weight = mul(diffuse_weight, rop);
+		specular_weight_rgb = mul(specular_weight_rgb, rop);
+	}
+	f3 dir_d = sample_psa<P>(pd, get_noise_2(seed), fa, biased);
+	f3 dir_s = mk3(0.0f, 0.0f, 1.0f);
+	if (ps.psa > 0.0f) {
+		dir_s = sample_psa<P>(ps, get_noise_2(seed), fa, biased);
+		dir_s = normalize<P>(mul(ltc.cosine_to_shading, dir_s));
+	}
+	const bool shadows = pr.shadows && pr.scene.triangle_count != 0;
+	uint32_t modes = 0;
+	for (int j = 0; j != technique_count; ++j) {
+		f3 dir = (j == 0) ? dir_d : dir_s;
+		if (dir.z <= 0.0f) continue;
+		float diffuse_density = dir.z * rcp_d;
+		float specular_density = evaluate_ltc_density<P>(ltc, dir, rcp_s);
+		f3 world_dir = transpose_mul(ltc.world_to_shading, dir);
+		const bool side = dot(sd.normal, world_dir) > 0.0f;
+		const bool traced = side && shadows;
+		const f3 rb_lit = side ? mul(l.radiance, evaluate_brdf<P>(sd, world_dir)) : splat(0.0f);
+		// Outcome 0: visible iff side (unoccluded or untraced); outcome 1:
+		// occluded.
+		for (int o = 0; o != (traced ? 2 : 1); ++o) {
+			const bool visibility = (o == 0) ? side : false;
+			f3 integrand = scale(visibility ? rb_lit : splat(0.0f), dir.z);
+			f3 r;
+			if (j == 0 && ps.psa <= 0.0f)
+				r = visibility ? scale(integrand, P::rcp(diffuse_density)) : splat(0.0f);
+			else if (j == 0)
+				r = mis_estimate<P>(pr.mis_heuristic, integrand, diffuse_weight, diffuse_density, specular_weight_rgb,
+				                    specular_density, pr.mis_visibility_estimate);
+			else
+				r = mis_estimate<P>(pr.mis_heuristic, integrand, specular_weight_rgb, specular_density, diffuse_weight,
+				                    diffuse_density, pr.mis_visibility_estimate);
+			if (j == 0) {
+				if (o == 0) c[0][0] = r; else c[0][1] = r;
+			} else {
+				if (o == 0) c[1][0] = r; else c[1][1] = r;
+			}
+		}
+		if (traced) {
+			// get_polygon_visibility, shading_pass.frag.glsl:112-129
+			float max_t = P::div(-plane_dot(sd.position, l.plane),
+			                     world_dir.x * l.plane[0] + world_dir.y * l.plane[1] + world_dir.z * l.plane[2]);
+			max_t -= 1e-3f;
+			const ShadowRay q{make_float4(sd.position.x, sd.position.y, sd.position.z, 0.0f),
+			                  make_float4(world_dir.x, world_dir.y, world_dir.z, max_t)};
+			if (j == 0) ray[0] = q; else ray[1] = q;
+		}
+		modes |= (traced ? kSampleTraced : kSampleFixed) << (2 * j);
+	}
+	return modes;
+}
+
+RL_DEV void store_sample(SampleRecord* dst, const f3 (&c)[2][2], float W, uint32_t flags) {
+	float4* q = reinterpret_cast<float4*>(dst);
+	q[0] = make_float4(c[0][0].x, c[0][0].y, c[0][0].z, c[0][1].x);
+	q[1] = make_float4(c[0][1].y, c[0][1].z, c[1][0].x, c[1][0].y);
+	q[2] = make_float4(c[1][0].z, c[1][1].x, c[1][1].y, c[1][1].z);
+	q[3] = make_float4(W, __uint_as_float(flags), 0.0f, 0.0f);
+}
+
+template <class P> __global__ void __launch_bounds__(128) ris_sample_kernel(RisParams pr) {
+	const uint32_t np = pr.width * pr.height;
+	ShadeParams sp;  // the fields psa_prepare_both and psa_mis_emit read
+	sp.scene = pr.scene;
+	sp.technique = sample_polygon_ltc_cp;
+	sp.mis_heuristic = pr.mis_heuristic;
+	sp.sample_count = 1;
+	sp.mis_visibility_estimate = pr.mis_visibility_estimate;
+	sp.fast_atan = pr.fast_atan;
+	sp.shadows = pr.shadows;
+	sp.error = pr.error;
+	const uint32_t lane = threadIdx.x % 32;
+	// The loop bound is uniform per block, so every warp reaches the ray
+	// queue's warp-wide scan converged.
+	for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
+		const uint32_t i = base + threadIdx.x;
+		const bool active = i < np && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
+		ShadingData sd;
+		Ltc ltc;
+		if (active) {
+			const float* g = pr.gbuffer;
+			const size_t snp = np;
+			sd.position = mk3(g[0 * snp + i], g[1 * snp + i], g[2 * snp + i]);
+			sd.normal = mk3(g[3 * snp + i], g[4 * snp + i], g[5 * snp + i]);
+			sd.outgoing = mk3(g[6 * snp + i], g[7 * snp + i], g[8 * snp + i]);
+			sd.lambert_outgoing = g[9 * snp + i];
+			sd.diffuse_albedo = mk3(g[10 * snp + i], g[11 * snp + i], g[12 * snp + i]);
+			sd.fresnel_0 = mk3(g[13 * snp + i], g[14 * snp + i], g[15 * snp + i]);
+			sd.roughness = g[16 * snp + i];
+			float fl = dot(sd.fresnel_0, mk3(0.2126f, 0.7152f, 0.0722f));
+			ltc = get_ltc_coefficients<P>(pr.scene, fl, sd.roughness, sd.position, sd.normal, sd.outgoing);
+		}
+		for (uint32_t f = 0; f != pr.frame_count; ++f) {
+			const size_t pf = (size_t) f * np + i;
+			uint32_t modes = 0;
+			ShadowRay ray[2];
+			if (active) {
+				const ReservoirRecord r = pr.records[pf];
+				f3 c[2][2];
+				c[0][0] = c[0][1] = c[1][0] = c[1][1] = splat(0.0f);
+				float W = 0.0f;
+				uint32_t flags = kSampleNoLight;
+				if (r.light_index >= 0) {
+					Light l;
+					load_light(pr.scene, r.light_index, l);
+					uint32_t seed = r.seed;
+					modes = psa_mis_emit<P>(sp, sd, ltc, l, seed, c, ray);
+					W = P::div(r.w_sum, (float) pr.candidate_count * r.p_hat);
+					if (r.p_hat == 0.0f) W = 0.0f;
+					flags = modes;
+				}
+				store_sample(pr.samples + pf, c, W, flags);
+			}
+			const uint32_t t0 = (modes & 3u) == kSampleTraced, t1 = ((modes >> 2) & 3u) == kSampleTraced;
+			// Warp-aggregated append to the ray queue.
+			__syncwarp();
+			const uint32_t count = t0 + t1;
+			uint32_t incl = count;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+				if ((int) lane >= d) incl += o;
+			}
+			const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+			uint32_t start = 0;
+			if (lane == 31 && total) start = atomicAdd(pr.ray_count, total);
+			start = __shfl_sync(0xffffffffu, start, 31);
+			uint32_t at = start + incl - count;
+			const uint32_t slot = 2u * (uint32_t) pf;
+			if (t0) {
+				ShadowRay q = ray[0];
+				q.origin_slot.w = __uint_as_float(slot);
+				pr.rays[at++] = q;
+			}
+			if (t1) {
+				ShadowRay q = ray[1];
+				q.origin_slot.w = __uint_as_float(slot + 1);
+				pr.rays[at] = q;
+			}
+		}
+	}
+}
+
+template <class P>
+__global__ void __launch_bounds__(128) shadow_trace_kernel(SceneView s, const ShadowRay* rays, const uint32_t* ray_count,
+                                                           uint8_t* hits, uint32_t* error) {
+	const uint32_t n = *ray_count;
+	for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+		const float4 a = __ldg(&rays[r].origin_slot), b = __ldg(&rays[r].dir_tmax);
+		const bool occluded = any_hit<P>(s, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), 1.0e-3f, b.w, error);
+		hits[__float_as_uint(a.w)] = occluded ? 1 : 0;
+	}
+}
+
+template <class P> __global__ void __launch_bounds__(128) ris_resolve_kernel(RisParams pr) {
+	const uint32_t np = pr.width * pr.height;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+		risltc_reservoir_t* res = pr.reservoirs ? pr.reservoirs + i : nullptr;
+		if (pr.primitive && pr.primitive[i] == 0xffffffffu) {
+			if (res) *res = risltc_reservoir_t{-1, 0.0f, 0.0f, 0u};
+			if (pr.out_rgb) {
+				pr.out_rgb[3 * (size_t) i + 0] = 0.0f;
+				pr.out_rgb[3 * (size_t) i + 1] = 0.0f;
+				pr.out_rgb[3 * (size_t) i + 2] = 0.0f;
+			}
+			continue;
+		}
+		f3 sum = splat(0.0f);
+		double acc[3] = {0.0, 0.0, 0.0};
+		for (uint32_t f = 0; f != pr.frame_count; ++f) {
+			const size_t pf = (size_t) f * np + i;
+			const float4* q = reinterpret_cast<const float4*>(pr.samples + pf);
+			const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+			const uint32_t flags = __float_as_uint(q3.y);
+			f3 final_color = splat(0.0f);
+			if (!(flags & kSampleNoLight)) {
+				const f3 c[2][2] = {{mk3(q0.x, q0.y, q0.z), mk3(q0.w, q1.x, q1.y)},
+				                    {mk3(q1.z, q1.w, q2.x), mk3(q2.y, q2.z, q2.w)}};
+				f3 result = splat(0.0f);
+#pragma unroll
+				for (int j = 0; j != 2; ++j) {
+					const uint32_t mode = (flags >> (2 * j)) & 3u;
+					if (mode == kSampleSkip) continue;
+					const bool occluded = mode == kSampleTraced && pr.hits[2 * pf + j] != 0;
+					result = add(result, occluded ? c[j][1] : c[j][0]);
+				}
+				const f3 color = scale(result, P::rcp(1.0f));
+				const f3 cw = scale(color, q3.x);
+				final_color = add(final_color, mk3(P::div(cw.x, 1.0f), P::div(cw.y, 1.0f), P::div(cw.z, 1.0f)));
+			}
+			if (isnan(final_color.x) || isnan(final_color.y) || isnan(final_color.z) || isinf(final_color.x) ||
+			    isinf(final_color.y) || isinf(final_color.z))
+				final_color = mk3(1.0f, 0.0f, 0.8f);
+			if (f == 0 && res) {
+				const ReservoirRecord r = pr.records[pf];
+				*res = risltc_reservoir_t{r.light_index, r.w_sum, r.p_hat, 0u};
+			}
+			sum = add(sum, final_color);
+			acc[0] += (double) final_color.x;
+			acc[1] += (double) final_color.y;
+			acc[2] += (double) final_color.z;
+		}
+		if (pr.out_rgb) {
+			f3 mean = pr.frame_count == 1 ? sum : scale(sum, 1.0f / (float) pr.frame_count);
+			pr.out_rgb[3 * (size_t) i + 0] = mean.x;
+			pr.out_rgb[3 * (size_t) i + 1] = mean.y;
+			pr.out_rgb[3 * (size_t) i + 2] = mean.z;
+		}
+		if (pr.accum) {
+			pr.accum[3 * (size_t) i + 0] += acc[0];
+			pr.accum[3 * (size_t) i + 1] += acc[1];
+			pr.accum[3 * (size_t) i + 2] += acc[2];
+		}
+	}
+}
+
+}  // namespace risltc

@@ -3,6 +3,7 @@
 // fused kernel's fast-candidate variant (its candidate loop uses hardware
 // reciprocal square root; its final shading stays exact).
 #include "ris_binned.cuh"
+#include "ris_wavefront.cuh"
 
 namespace risltc {
 cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast) {
@@ -12,10 +13,8 @@ cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cu
 	else
 		shade_kernel<ExactNumerics, ExactNumerics><<<grid, 128, 0, stream>>>(p);
 	cudaError_t e = cudaGetLastError();
-	if (events) {
-		cudaEventRecord(events[1], stream);
-		cudaEventRecord(events[2], stream);
-	}
+	if (events)
+		for (int k = 1; k != 5; ++k) cudaEventRecord(events[k], stream);
 	return e;
 }
 cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid) {
@@ -28,6 +27,18 @@ cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int
 }
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid) {
 	ris_shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	return cudaGetLastError();
+}
+cudaError_t launch_ris_sample(const RisParams& p, cudaStream_t stream, int grid) {
+	ris_sample_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	return cudaGetLastError();
+}
+cudaError_t launch_shadow_trace(const RisParams& p, cudaStream_t stream, int grid) {
+	shadow_trace_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p.scene, p.rays, p.ray_count, p.hits, p.error);
+	return cudaGetLastError();
+}
+cudaError_t launch_ris_resolve(const RisParams& p, cudaStream_t stream, int grid) {
+	ris_resolve_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
 	return cudaGetLastError();
 }
 cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,

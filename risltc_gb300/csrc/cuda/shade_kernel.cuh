@@ -135,14 +135,16 @@ template <class P> RL_DEV f3 ltc_cp_target(const ShadingData& sd, Ltc ltc, const
 // evaluate_polygonal_light_shading_peters (peters = true,
 // shading_pass.frag.glsl:292-397) and the PSA branch of
 // evaluate_polygonal_light_shading (peters = false, :458-550)
+// The side flip and both polygons' PSA sampling preparations of
+// evaluate_polygonal_light_shading_peters (shading_pass.frag.glsl:298-341):
+// pd in shading space, ps in cosine space.  Returns false when the estimate
+// is zero (the polygon clips to nothing or has no projected solid angle in
+// shading space).
 template <class P>
-RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l, uint32_t& seed,
-                        bool peters, bool visibility_in) {
+RL_DEV bool psa_prepare_both(const ShadeParams& pr, const ShadingData& sd, Ltc& ltc, const Light& l, PsaPolygon& pd,
+                             PsaPolygon& ps) {
 	const bool fa = pr.fast_atan != 0;
-	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
-	f3 result = splat(0.0f);
 	side_flip(ltc, sd, l);
-	PsaPolygon pd, ps;
 	uint32_t n = l.vertex_count;
 	for (int i = 0; i != 2; ++i) {
 		mat43 w2l = (i == 0) ? ltc.world_to_shading : mul(ltc.shading_to_cosine, ltc.world_to_shading);
@@ -151,7 +153,7 @@ RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, c
 		for (int j = 0; j != kMaxLightVertices; ++j)
 			if (j < (int) n) verts[j] = mul_point(w2l, l.v[j]);
 		uint32_t vc = clip_polygon<P>(n, verts);
-		if (vc == 0 && i == 0) return result;
+		if (vc == 0 && i == 0) return false;
 		if (vc == 0) {
 			ps.psa = 0.0f;
 			break;
@@ -161,7 +163,17 @@ RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, c
 		else
 			prepare_psa<P>(ps, vc, verts, fa);
 	}
-	if (pd.psa == 0.0f) return result;
+	return pd.psa != 0.0f;
+}
+
+template <class P>
+RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l, uint32_t& seed,
+                        bool peters, bool visibility_in) {
+	const bool fa = pr.fast_atan != 0;
+	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
+	f3 result = splat(0.0f);
+	PsaPolygon pd, ps;
+	if (!psa_prepare_both<P>(pr, sd, ltc, l, pd, ps)) return result;
 	float specular_weight = ltc.albedo * ps.psa;
 	f3 diffuse_weight = scale(max3(sd.diffuse_albedo, splat(0.01f)), pd.psa);
 	int technique_count = (ps.psa > 0.0f) ? 2 : 1;
