@@ -26,14 +26,19 @@ struct risltc_ctx_s {
 	// Reservoir records between the candidate and shading kernels.
 	risltc::ReservoirRecord* d_records;
 	size_t record_capacity;
-	// The shading phase's state between its sample, shadow-trace and resolve
-	// kernels: a 64-byte sample record per pixel-frame, a queue of up to two
-	// 32-byte shadow rays per pixel-frame, their outcomes and the queue length.
+	// The shading phase's state between its sample, shadow-ray and resolve
+	// kernels: a 64-byte sample record per pixel-frame, up to two 32-byte
+	// shadow rays per pixel-frame (as staged, then grouped by light), their
+	// outcomes, the queue length and fetch cursor, and the per-light bucket
+	// counters.
 	risltc::SampleRecord* d_samples;
+	risltc::ShadowRay* d_staged;
 	risltc::ShadowRay* d_rays;
 	uint8_t* d_hits;
 	uint32_t* d_ray_count;
+	uint32_t* d_light_rays;
 	size_t wavefront_capacity;
+	size_t light_capacity;
 	// Kernel timing: five events per shading call (before, between and after
 	// the phases), up to 64 calls between queries.
 	int profiling;
@@ -47,7 +52,7 @@ struct risltc_scene_s {
 	risltc::SceneView view;
 	void* d_lights;
 	void* d_ltc;
-	void* d_nodes;
+	void* d_pairs;
 	void* d_triangles;
 	uint32_t max_vertex_count;
 	uint32_t bvh_depth;
@@ -70,19 +75,69 @@ int grid_for(const risltc_ctx_t* ctx, size_t items) {
 	return (int) (blocks ? blocks : 1);
 }
 
-int reserve_wavefront(risltc_ctx_t* ctx, size_t pixel_frames) {
+// The BVH's device layout for traversal: the root's record {bmin, reference,
+// bmax, triangle count} (8 floats), then one 16-float record per inner node
+// holding both children's records.  A reference is an inner node's record
+// index or a leaf's first triangle; the count is 0 for an inner node.  Inner
+// nodes are numbered depth first, so a left child follows its parent.
+// nodes: risltc_bvh_t's 8-float nodes {bmin, left child or first triangle,
+// bmax, count}, the children of an inner node adjacent.
+std::vector<float> child_pair_nodes(const float* nodes, uint32_t node_count) {
+	auto word = [&](uint32_t n, int k) {
+		int32_t w;
+		memcpy(&w, nodes + 8 * (size_t) n + k, sizeof(w));
+		return w;
+	};
+	std::vector<int32_t> index(node_count, -1);
+	std::vector<uint32_t> order, stack{0};
+	while (!stack.empty()) {
+		const uint32_t n = stack.back();
+		stack.pop_back();
+		if (word(n, 7) != 0) continue;
+		index[n] = (int32_t) order.size();
+		order.push_back(n);
+		stack.push_back((uint32_t) word(n, 3) + 1);
+		stack.push_back((uint32_t) word(n, 3));
+	}
+	std::vector<float> out(8 + 16 * order.size());
+	auto put = [&](float* dst, uint32_t c) {
+		memcpy(dst, nodes + 8 * (size_t) c, 8 * sizeof(float));
+		const int32_t ref = word(c, 7) == 0 ? index[c] : word(c, 3);
+		memcpy(dst + 3, &ref, sizeof(ref));
+	};
+	put(out.data(), 0);
+	for (size_t k = 0; k != order.size(); ++k) {
+		const uint32_t first = (uint32_t) word(order[k], 3);
+		put(out.data() + 8 + 16 * k, first);
+		put(out.data() + 8 + 16 * k + 8, first + 1);
+	}
+	return out;
+}
+
+int reserve_wavefront(risltc_ctx_t* ctx, size_t pixel_frames, size_t light_count) {
+	cudaError_t e = cudaSuccess;
+	if (light_count > ctx->light_capacity) {
+		cudaStreamSynchronize(ctx->stream);
+		cudaFree(ctx->d_light_rays);
+		ctx->d_light_rays = nullptr;
+		ctx->light_capacity = 0;
+		if ((e = cudaMalloc(&ctx->d_light_rays, light_count * sizeof(uint32_t))) != cudaSuccess) return cuda_status(e);
+		ctx->light_capacity = light_count;
+	}
 	if (pixel_frames <= ctx->wavefront_capacity) return RISLTC_OK;
 	cudaStreamSynchronize(ctx->stream);
 	cudaFree(ctx->d_samples);
+	cudaFree(ctx->d_staged);
 	cudaFree(ctx->d_rays);
 	cudaFree(ctx->d_hits);
 	ctx->d_samples = nullptr;
+	ctx->d_staged = nullptr;
 	ctx->d_rays = nullptr;
 	ctx->d_hits = nullptr;
 	ctx->wavefront_capacity = 0;
-	cudaError_t e = cudaSuccess;
-	if (!ctx->d_ray_count) e = cudaMalloc(&ctx->d_ray_count, sizeof(uint32_t));
+	if (!ctx->d_ray_count) e = cudaMalloc(&ctx->d_ray_count, 2 * sizeof(uint32_t));
 	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_samples, pixel_frames * sizeof(risltc::SampleRecord));
+	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_staged, 2 * pixel_frames * sizeof(risltc::ShadowRay));
 	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rays, 2 * pixel_frames * sizeof(risltc::ShadowRay));
 	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_hits, 2 * pixel_frames);
 	if (e != cudaSuccess) return cuda_status(e);
@@ -126,9 +181,11 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFreeHost(ctx->h_pinned_rgb);
 	cudaFree(ctx->d_records);
 	cudaFree(ctx->d_samples);
+	cudaFree(ctx->d_staged);
 	cudaFree(ctx->d_rays);
 	cudaFree(ctx->d_hits);
 	cudaFree(ctx->d_ray_count);
+	cudaFree(ctx->d_light_rays);
 	for (int i = 0; i < ctx->events_created; ++i)
 		for (int k = 0; k != 5; ++k) cudaEventDestroy(ctx->events[i][k]);
 	free(ctx);
@@ -195,7 +252,8 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	upload(&scene->d_lights, lights.data(), lights.size() * sizeof(float));
 	upload(&scene->d_ltc, ltc_dev.data(), ltc_dev.size() * sizeof(float));
 	if (triangle_count) {
-		upload(&scene->d_nodes, bvh.nodes, (size_t) bvh.node_count * 8 * sizeof(float));
+		const std::vector<float> pairs = child_pair_nodes(bvh.nodes, bvh.node_count);
+		upload(&scene->d_pairs, pairs.data(), pairs.size() * sizeof(float));
 		upload(&scene->d_triangles, bvh.triangles, (size_t) bvh.triangle_count * 12 * sizeof(float));
 	}
 	risltc_bvh_destroy(&bvh);
@@ -216,7 +274,7 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	v.ltc_constants[3] = ltc->constants.roughness_summand;
 	v.ltc_constants[4] = ltc->constants.inclination_factor;
 	v.ltc_constants[5] = ltc->constants.inclination_summand;
-	v.nodes = (const float4*) scene->d_nodes;
+	v.pairs = (const float4*) scene->d_pairs;
 	v.triangles = (const float4*) scene->d_triangles;
 	v.triangle_count = (int) triangle_count;
 	*out = scene;
@@ -232,7 +290,7 @@ EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene) {
 	cudaStreamSynchronize(scene->ctx->stream);
 	cudaFree(scene->d_lights);
 	cudaFree(scene->d_ltc);
-	cudaFree(scene->d_nodes);
+	cudaFree(scene->d_pairs);
 	cudaFree(scene->d_triangles);
 	free(scene);
 }
@@ -324,10 +382,12 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		const size_t pixel_frames = pixels * frame_count;
 		if (settings->shadows && scene->view.triangle_count && settings->sample_count == 1 &&
 		    pixel_frames < (1ull << 31)) {
-			st = reserve_wavefront(ctx, pixel_frames);
+			st = reserve_wavefront(ctx, pixel_frames, scene->view.light_count);
 			if (st) return st;
 			r.samples = ctx->d_samples;
+			r.staged = ctx->d_staged;
 			r.rays = ctx->d_rays;
+			r.light_rays = ctx->d_light_rays;
 			r.ray_count = ctx->d_ray_count;
 			r.hits = ctx->d_hits;
 		}

@@ -29,7 +29,7 @@ namespace risltc {
 #define RISLTC_BINNED_CHUNK 8
 #endif
 #ifndef RISLTC_BINNED_MIN_BLOCKS
-#define RISLTC_BINNED_MIN_BLOCKS 5
+#define RISLTC_BINNED_MIN_BLOCKS 4
 #endif
 constexpr int kChunk = RISLTC_BINNED_CHUNK;  // candidates per pixel per chunk
 constexpr int kItems = 32 * kChunk;          // items per warp per chunk
@@ -72,10 +72,35 @@ RL_DEV void store_frame(float* f, const CandidateFrame& cf) {
 	}
 }
 
+// A light vertex (slot j of the record) in local space: mat4x3 * vec4(v, 1)
+// with y negated when negate_y is set (the side flip).
+RL_DEV f3 local_vertex(const mat43& t, const float4* record, uint32_t j, bool negate_y) {
+	const float4 q = __ldg(record + 2 + j);
+	f3 v = mul_point(t, mk3(q.x, q.y, q.z));
+	v.y = negate_y ? -v.y : v.y;
+	return v;
+}
+
+// The partially clipped case: clip_polygon, then calculate_ltc; -1 when the
+// polygon clips to nothing.  Kept out of line (about 1% of candidates).
+template <class P>
+__device__ __noinline__ float clipped_integral(mat43 t, const float4* record, uint32_t n, bool negate_y) {
+	f3 v[kMaxPolygonVertices];
+#pragma unroll
+	for (int j = 0; j != kMaxLightVertices; ++j) v[j] = local_vertex(t, record, (uint32_t) j, negate_y);
+	const uint32_t vc = clip_polygon<P>(n, v);
+	return vc > 0 ? calculate_ltc<P>(vc, v) : -1.0f;
+}
+
 // One candidate (ltc_cp_candidate, then p_hat = length(color)) with the
 // frame in shared memory.  The two LTC integrals run in one loop over the
-// spaces to keep the code small.  With allow_clip false, returns false as
-// soon as a space clips the polygon partially; the caller defers the item.
+// spaces, and each polygon is streamed vertex by vertex from the light
+// record: a first pass counts the vertices above the horizon, a second
+// transforms, normalises and integrates edge after edge in the order of
+// calculate_ltc (edges 0-1, ..., (n-2)-(n-1), then (n-1)-0).  The code stays
+// small and the vertex count of a sorted group is uniform across the warp.
+// With allow_clip false, returns false as soon as a space clips the polygon
+// partially; the caller defers the item.
 template <class P>
 RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
 	const float4 head = __ldg(record), pl = __ldg(record + 1);
@@ -91,23 +116,26 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 #pragma unroll
 		for (int c = 0; c != 4; ++c) t.c[c] = mk3(m[3 * c], m[3 * c + 1], m[3 * c + 2]);
 		const bool negate_y = s == 0 && flip;
-		PolygonVerts v;
 		uint32_t above = 0;
-#pragma unroll
-		for (int j = 0; j != kMaxLightVertices; ++j) {
-			const float4 q = __ldg(record + 2 + j);
-			v.v[j] = mul_point(t, mk3(q.x, q.y, q.z));
-			v.v[j].y = negate_y ? -v.v[j].y : v.v[j].y;
-			if (j < (int) n && v.v[j].z > 0.0f) ++above;
-		}
+#pragma unroll 1
+		for (uint32_t j = 0; j != n; ++j) above += local_vertex(t, record, j, negate_y).z > 0.0f ? 1u : 0u;
 		const bool partial = above != 0 && above != n;
 		if (partial && !allow_clip) return false;
 		float r = 0.0f;
 		bool a = above == 0;
 		if (above == n) {
-			r = ltc_integral_unclipped<P>(v.v, n);
+			const f3 first = normalize<P>(local_vertex(t, record, 0, negate_y));
+			f3 prev = first;
+#pragma unroll 1
+			for (uint32_t j = 1; j != n; ++j) {
+				const f3 cur = normalize<P>(local_vertex(t, record, j, negate_y));
+				r += integrate_edge<P>(prev, cur);
+				prev = cur;
+			}
+			r += integrate_edge<P>(prev, first);
+			r = fabsf(r);
 		} else if (partial) {
-			r = ltc_integral_clipped<P>(v, n);
+			r = clipped_integral<P>(t, record, n, negate_y);
 			a = r < 0.0f;
 			r = a ? 0.0f : r;
 		}

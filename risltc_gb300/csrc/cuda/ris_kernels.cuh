@@ -40,8 +40,10 @@ struct RisParams {
 	ReservoirRecord* records;  // [frame][pixel] scratch
 	// Shadow rays traced in their own pass (null: traced in ris_shade_kernel).
 	struct SampleRecord* samples;  // [frame][pixel]
-	struct ShadowRay* rays;        // compacted queue, up to 2 per pixel-frame
-	uint32_t* ray_count;           // queue length (zeroed before the sample pass)
+	struct ShadowRay* staged;      // [frame][pixel][technique], as generated
+	struct ShadowRay* rays;        // the traced ones grouped by light
+	uint32_t* light_rays;          // per light: ray count, then bucket cursor
+	uint32_t* ray_count;           // [queue length, trace fetch cursor]
 	uint8_t* hits;                 // [frame][pixel][technique] occlusion
 	float* out_rgb;
 	double* accum;
@@ -287,12 +289,13 @@ cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int
 cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_ris_sample(const RisParams& p, cudaStream_t stream, int grid);
+cudaError_t launch_shadow_sort(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_shadow_trace(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_ris_resolve(const RisParams& p, cudaStream_t stream, int grid);
 
 // The candidate kernel (fast or exact numerics), then the shading phase
-// (always exact): ris_shade_kernel, or with p.samples set the sample, shadow
-// trace and resolve kernels.  events (may be null) holds five events,
+// (always exact): ris_shade_kernel, or with p.samples set the sample kernel,
+// the shadow rays' grouping by light and trace, and the resolve kernel.  events (may be null) holds five events,
 // recorded before, between and after the phases (the last three together for
 // ris_shade_kernel).
 inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid, int trace_grid, cudaEvent_t* events,
@@ -302,11 +305,12 @@ inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid,
 	if (e != cudaSuccess) return e;
 	if (events) cudaEventRecord(events[1], stream);
 	if (p.samples) {
-		e = cudaMemsetAsync(p.ray_count, 0, sizeof(uint32_t), stream);
+		e = cudaMemsetAsync(p.light_rays, 0, sizeof(uint32_t) * p.scene.light_count, stream);
 		if (e == cudaSuccess) e = launch_ris_sample(p, stream, grid);
 		if (e != cudaSuccess) return e;
 		if (events) cudaEventRecord(events[2], stream);
-		e = launch_shadow_trace(p, stream, trace_grid);
+		e = launch_shadow_sort(p, stream, grid);
+		if (e == cudaSuccess) e = launch_shadow_trace(p, stream, trace_grid);
 		if (e != cudaSuccess) return e;
 		if (events) cudaEventRecord(events[3], stream);
 		e = launch_ris_resolve(p, stream, grid);

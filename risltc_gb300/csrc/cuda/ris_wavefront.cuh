@@ -5,7 +5,10 @@
 //     evaluate_polygonal_light_shading_peters (shading_pass.frag.glsl:292-397)
 //     for the chosen light up to the visibility test.  For each of its (at
 //     most two) samples it stores the MIS-weighted contribution for both
-//     outcomes of the shadow ray and appends the ray to a compacted queue.
+//     outcomes of the shadow ray and stages the ray.
+//   light_bucket_scan_kernel, shadow_scatter_kernel: group the rays by light
+//     (a counting sort), so that the rays of one warp start near each other
+//     and aim at the same polygon.
 //   shadow_trace_kernel: one any-hit query per queued ray, with a small
 //     register footprint and no divergence from the shading code around it.
 //   ris_resolve_kernel: per pixel, picks each sample's contribution by its
@@ -134,9 +137,6 @@ template <class P> __global__ void __launch_bounds__(128) ris_sample_kernel(RisP
 	sp.fast_atan = pr.fast_atan;
 	sp.shadows = pr.shadows;
 	sp.error = pr.error;
-	const uint32_t lane = threadIdx.x % 32;
-	// The loop bound is uniform per block, so every warp reaches the ray
-	// queue's warp-wide scan converged.
 	for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
 		const uint32_t i = base + threadIdx.x;
 		const bool active = i < np && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
@@ -176,44 +176,133 @@ template <class P> __global__ void __launch_bounds__(128) ris_sample_kernel(RisP
 				}
 				store_sample(pr.samples + pf, c, W, flags);
 			}
-			const uint32_t t0 = (modes & 3u) == kSampleTraced, t1 = ((modes >> 2) & 3u) == kSampleTraced;
-			// Warp-aggregated append to the ray queue.
-			__syncwarp();
-			const uint32_t count = t0 + t1;
-			uint32_t incl = count;
-#pragma unroll
-			for (int d = 1; d < 32; d <<= 1) {
-				const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
-				if ((int) lane >= d) incl += o;
-			}
-			const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-			uint32_t start = 0;
-			if (lane == 31 && total) start = atomicAdd(pr.ray_count, total);
-			start = __shfl_sync(0xffffffffu, start, 31);
-			uint32_t at = start + incl - count;
-			const uint32_t slot = 2u * (uint32_t) pf;
-			if (t0) {
-				ShadowRay q = ray[0];
-				q.origin_slot.w = __uint_as_float(slot);
-				pr.rays[at++] = q;
-			}
-			if (t1) {
-				ShadowRay q = ray[1];
-				q.origin_slot.w = __uint_as_float(slot + 1);
-				pr.rays[at] = q;
-			}
+			// Stage the rays in their pixel-frame's slots and count them for
+			// their light's bucket.
+			const bool t0 = (modes & 3u) == kSampleTraced, t1 = ((modes >> 2) & 3u) == kSampleTraced;
+			if (t0) pr.staged[2 * pf] = ray[0];
+			if (t1) pr.staged[2 * pf + 1] = ray[1];
+			if (t0 || t1) atomicAdd(pr.light_rays + pr.records[pf].light_index, (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
 		}
 	}
 }
 
+// Exclusive prefix sum of the per-light ray counts, in place (each becomes
+// its bucket's first queue position); the total goes to ray_count[0] and the
+// trace kernel's fetch cursor ray_count[1] is reset.  One block of 1024
+// threads.
+static __global__ void __launch_bounds__(1024) light_bucket_scan_kernel(uint32_t* light_rays, uint32_t light_count,
+                                                                 uint32_t* ray_count) {
+	__shared__ uint32_t warp_offset[32];
+	__shared__ uint32_t chunk_total;
+	const uint32_t lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+	uint32_t carry = 0;
+	for (uint32_t base = 0; base < light_count; base += 1024) {
+		const uint32_t i = base + threadIdx.x;
+		const uint32_t v = i < light_count ? light_rays[i] : 0u;
+		uint32_t incl = v;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+			if ((int) lane >= d) incl += o;
+		}
+		if (lane == 31) warp_offset[warp] = incl;
+		__syncthreads();
+		if (warp == 0) {
+			const uint32_t w = warp_offset[lane];
+			uint32_t wi = w;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				const uint32_t o = __shfl_up_sync(0xffffffffu, wi, d);
+				if ((int) lane >= d) wi += o;
+			}
+			warp_offset[lane] = wi - w;
+			if (lane == 31) chunk_total = wi;
+		}
+		__syncthreads();
+		if (i < light_count) light_rays[i] = carry + warp_offset[warp] + incl - v;
+		carry += chunk_total;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		ray_count[0] = carry;
+		ray_count[1] = 0;  // the trace kernel's fetch cursor
+	}
+}
+
+// Moves the staged rays into their light's bucket, tagging each with its hit
+// slot.
+static __global__ void __launch_bounds__(128) shadow_scatter_kernel(RisParams pr) {
+	const uint32_t np = pr.width * pr.height;
+	const size_t total = (size_t) np * pr.frame_count;
+	for (size_t pf = blockIdx.x * (size_t) blockDim.x + threadIdx.x; pf < total; pf += (size_t) gridDim.x * blockDim.x) {
+		const uint32_t i = (uint32_t) (pf % np);
+		if (pr.primitive && pr.primitive[i] == 0xffffffffu) continue;
+		const uint32_t flags = __float_as_uint(reinterpret_cast<const float4*>(pr.samples + pf)[3].y);
+		if (flags & kSampleNoLight) continue;
+		const bool t0 = (flags & 3u) == kSampleTraced, t1 = ((flags >> 2) & 3u) == kSampleTraced;
+		if (!t0 && !t1) continue;
+		uint32_t at = atomicAdd(pr.light_rays + pr.records[pf].light_index, (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
+		const uint32_t slot = 2u * (uint32_t) pf;
+		if (t0) {
+			ShadowRay q = pr.staged[2 * pf];
+			q.origin_slot.w = __uint_as_float(slot);
+			pr.rays[at++] = q;
+		}
+		if (t1) {
+			ShadowRay q = pr.staged[2 * pf + 1];
+			q.origin_slot.w = __uint_as_float(slot + 1);
+			pr.rays[at] = q;
+		}
+	}
+}
+
+#ifndef RISLTC_TRACE_REFILL
+#define RISLTC_TRACE_REFILL 8
+#endif
+// Persistent any-hit tracing of the queue (queue[0] rays; queue[1] is the
+// fetch cursor, zero at launch).  Each lane holds one ray and advances it one
+// inner node per iteration; whenever RISLTC_TRACE_REFILL or more lanes of a
+// warp are idle they fetch the next rays together, so lanes do not wait for
+// the warp's longest ray.
 template <class P>
-__global__ void __launch_bounds__(128) shadow_trace_kernel(SceneView s, const ShadowRay* rays, const uint32_t* ray_count,
+__global__ void __launch_bounds__(128) shadow_trace_kernel(SceneView s, const ShadowRay* rays, uint32_t* queue,
                                                            uint8_t* hits, uint32_t* error) {
-	const uint32_t n = *ray_count;
-	for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-		const float4 a = __ldg(&rays[r].origin_slot), b = __ldg(&rays[r].dir_tmax);
-		const bool occluded = any_hit<P>(s, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), 1.0e-3f, b.w, error);
-		hits[__float_as_uint(a.w)] = occluded ? 1 : 0;
+	const uint32_t n = queue[0];
+	const uint32_t lane = threadIdx.x % 32;
+	int32_t stack[kBvhStack];
+	TraceRay r;
+	uint32_t slot = 0;
+	bool busy = false, drained = false;
+	for (;;) {
+		const uint32_t idle = __ballot_sync(0xffffffffu, !busy);
+		if (drained && idle == 0xffffffffu) break;
+		if (!drained && __popc(idle) >= RISLTC_TRACE_REFILL) {
+			const int leader = __ffs(idle) - 1;
+			uint32_t base = 0;
+			if ((int) lane == leader) base = atomicAdd(queue + 1, (uint32_t) __popc(idle));
+			base = __shfl_sync(0xffffffffu, base, leader);
+			drained = base + (uint32_t) __popc(idle) >= n;
+			if (!busy) {
+				const uint32_t k = base + (uint32_t) __popc(idle & ((1u << lane) - 1u));
+				if (k < n) {
+					const float4 a = __ldg(&rays[k].origin_slot), b = __ldg(&rays[k].dir_tmax);
+					slot = __float_as_uint(a.w);
+					const int st = trace_begin<P>(s, r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), 1.0e-3f, b.w);
+					if (st == kTraceContinue)
+						busy = true;
+					else
+						hits[slot] = st == kTraceHit ? 1 : 0;
+				}
+			}
+			continue;
+		}
+		if (busy) {
+			const int st = trace_step<P>(s, r, stack, error);
+			if (st != kTraceContinue) {
+				hits[slot] = st == kTraceHit ? 1 : 0;
+				busy = false;
+			}
+		}
 	}
 }
 

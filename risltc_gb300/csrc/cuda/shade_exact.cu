@@ -33,6 +33,13 @@ cudaError_t launch_ris_sample(const RisParams& p, cudaStream_t stream, int grid)
 	ris_sample_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
 	return cudaGetLastError();
 }
+cudaError_t launch_shadow_sort(const RisParams& p, cudaStream_t stream, int grid) {
+	light_bucket_scan_kernel<<<1, 1024, 0, stream>>>(p.light_rays, (uint32_t) p.scene.light_count, p.ray_count);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	shadow_scatter_kernel<<<grid, 128, 0, stream>>>(p);
+	return cudaGetLastError();
+}
 cudaError_t launch_shadow_trace(const RisParams& p, cudaStream_t stream, int grid) {
 	shadow_trace_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p.scene, p.rays, p.ray_count, p.hits, p.error);
 	return cudaGetLastError();

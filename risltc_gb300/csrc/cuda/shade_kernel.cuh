@@ -33,64 +33,125 @@ struct ShadeParams {
 	uint32_t* error;             // error bits (atomicOr)
 };
 
-// Any-hit query against the BVH (stack traversal, near child first is not
-// needed for any-hit).  Returns true if occluded.  Gives up after
-// kTraversalLimit node visits, records the error and reports "not occluded".
-template <class P> RL_DEV bool any_hit(const SceneView& s, f3 o, f3 d, float t_min, float t_max, uint32_t* error) {
-	if (s.triangle_count == 0) return false;
-	float inv[3] = {P::rcp(d.x), P::rcp(d.y), P::rcp(d.z)};
-	float org[3] = {o.x, o.y, o.z};
-	int32_t stack[kBvhStack];
-	int sp = 0;
-	stack[sp++] = 0;
-	uint32_t visits = 0;
-	while (sp > 0) {
-		if (++visits > kTraversalLimit) {
-			atomicOr(error, kErrorTraversalLimit);
-			return false;
-		}
-		int32_t ni = stack[--sp];
-		float4 a = __ldg(s.nodes + 2 * (size_t) ni), b = __ldg(s.nodes + 2 * (size_t) ni + 1);
-		float lo = t_min, hi = t_max;
-		float bmin[3] = {a.x, a.y, a.z}, bmax[3] = {b.x, b.y, b.z};
+// Any-hit traversal of the BVH in its child-pair layout (SceneView::pairs):
+// every step loads one inner node with both children's boxes, tests the
+// triangles of the hit leaf children at once and descends into a hit inner
+// child, keeping the other on a stack.  A triangle is tested exactly when
+// every box on its path is hit, so the answer equals a brute-force test of
+// all triangles given conservative boxes; only the order of the tests
+// differs, which an any-hit query does not see.
+struct TraceRay {
+	f3 o, d;
+	float inv[3];
+	float t_min, t_max;
+	int32_t node;     // the inner node to visit next
+	int sp;
+	uint32_t visits;
+};
+
+enum : int { kTraceContinue = 0, kTraceMiss = 1, kTraceHit = 2 };
+
+// Slab test of one box against the ray's [t_min, t_max].
+RL_DEV bool ray_box(const TraceRay& r, float4 lo, float4 hi) {
+	const float bmin[3] = {lo.x, lo.y, lo.z}, bmax[3] = {hi.x, hi.y, hi.z};
+	const float org[3] = {r.o.x, r.o.y, r.o.z};
+	float t0s = r.t_min, t1s = r.t_max;
 #pragma unroll
-		for (int ax = 0; ax != 3; ++ax) {
-			float t0 = (bmin[ax] - org[ax]) * inv[ax];
-			float t1 = (bmax[ax] - org[ax]) * inv[ax];
-			float tn = t0 < t1 ? t0 : t1, tf = t0 < t1 ? t1 : t0;
-			if (tn == tn && tn > lo) lo = tn;
-			if (tf == tf && tf < hi) hi = tf;
-		}
-		if (!(lo <= hi)) continue;
-		int32_t first = __float_as_int(a.w), count = __float_as_int(b.w);
-		if (count == 0) {
-			if (sp + 2 > kBvhStack) {
-				atomicOr(error, kErrorTraversalLimit);
-				return false;
-			}
-			stack[sp++] = first + 1;
-			stack[sp++] = first;
-		} else {
-			for (int k = 0; k != count; ++k) {
-				const float4* t = s.triangles + 3 * (size_t) (first + k);
-				float4 q0 = __ldg(t), q1 = __ldg(t + 1), q2 = __ldg(t + 2);
-				f3 v0 = mk3(q0.x, q0.y, q0.z), e1 = mk3(q1.x, q1.y, q1.z), e2 = mk3(q2.x, q2.y, q2.z);
-				f3 p = cross(d, e2);
-				float det = dot(e1, p);
-				if (!(det != 0.0f)) continue;
-				float id = P::rcp(det);
-				f3 sv = sub(o, v0);
-				float u = dot(sv, p) * id;
-				if (!(u >= 0.0f && u <= 1.0f)) continue;
-				f3 q = cross(sv, e1);
-				float v = dot(d, q) * id;
-				if (!(v >= 0.0f && u + v <= 1.0f)) continue;
-				float tt = dot(e2, q) * id;
-				if (tt >= t_min && tt <= t_max) return true;
-			}
-		}
+	for (int ax = 0; ax != 3; ++ax) {
+		float t0 = (bmin[ax] - org[ax]) * r.inv[ax];
+		float t1 = (bmax[ax] - org[ax]) * r.inv[ax];
+		float tn = t0 < t1 ? t0 : t1, tf = t0 < t1 ? t1 : t0;
+		if (tn == tn && tn > t0s) t0s = tn;
+		if (tf == tf && tf < t1s) t1s = tf;
 	}
+	return t0s <= t1s;
+}
+
+// Moller-Trumbore with the triangle stored as {v0, e1, e2}; a hit with t in
+// [t_min, t_max] counts.
+template <class P> RL_DEV bool ray_triangle(const TraceRay& r, const float4* t) {
+	const float4 q0 = __ldg(t), q1 = __ldg(t + 1), q2 = __ldg(t + 2);
+	const f3 v0 = mk3(q0.x, q0.y, q0.z), e1 = mk3(q1.x, q1.y, q1.z), e2 = mk3(q2.x, q2.y, q2.z);
+	const f3 p = cross(r.d, e2);
+	const float det = dot(e1, p);
+	if (!(det != 0.0f)) return false;
+	const float id = P::rcp(det);
+	const f3 sv = sub(r.o, v0);
+	const float u = dot(sv, p) * id;
+	if (!(u >= 0.0f && u <= 1.0f)) return false;
+	const f3 q = cross(sv, e1);
+	const float v = dot(r.d, q) * id;
+	if (!(v >= 0.0f && u + v <= 1.0f)) return false;
+	const float tt = dot(e2, q) * id;
+	return tt >= r.t_min && tt <= r.t_max;
+}
+
+template <class P> RL_DEV bool ray_leaf(const SceneView& s, const TraceRay& r, int32_t first, int32_t count) {
+	for (int32_t k = 0; k != count; ++k)
+		if (ray_triangle<P>(r, s.triangles + 3 * (size_t) (first + k))) return true;
 	return false;
+}
+
+// Sets up the ray and tests the root: returns kTraceContinue with r.node set,
+// or the answer when the root is missed or is a leaf.
+template <class P> RL_DEV int trace_begin(const SceneView& s, TraceRay& r, f3 o, f3 d, float t_min, float t_max) {
+	r.o = o;
+	r.d = d;
+	r.inv[0] = P::rcp(d.x);
+	r.inv[1] = P::rcp(d.y);
+	r.inv[2] = P::rcp(d.z);
+	r.t_min = t_min;
+	r.t_max = t_max;
+	r.sp = 0;
+	r.visits = 0;
+	if (s.triangle_count == 0) return kTraceMiss;
+	const float4 lo = __ldg(s.pairs), hi = __ldg(s.pairs + 1);
+	if (!ray_box(r, lo, hi)) return kTraceMiss;
+	const int32_t ref = __float_as_int(lo.w), count = __float_as_int(hi.w);
+	if (count != 0) return ray_leaf<P>(s, r, ref, count) ? kTraceHit : kTraceMiss;
+	r.node = ref;
+	return kTraceContinue;
+}
+
+// One inner node.  Gives up after kTraversalLimit steps or on a stack
+// overflow, records the error and reports "not occluded".
+template <class P> RL_DEV int trace_step(const SceneView& s, TraceRay& r, int32_t* stack, uint32_t* error) {
+	if (++r.visits > kTraversalLimit) {
+		atomicOr(error, kErrorTraversalLimit);
+		return kTraceMiss;
+	}
+	const float4* n = s.pairs + 2 + 4 * (size_t) r.node;
+	const float4 lo0 = __ldg(n), hi0 = __ldg(n + 1), lo1 = __ldg(n + 2), hi1 = __ldg(n + 3);
+	const bool h0 = ray_box(r, lo0, hi0), h1 = ray_box(r, lo1, hi1);
+	const int32_t ref0 = __float_as_int(lo0.w), count0 = __float_as_int(hi0.w);
+	const int32_t ref1 = __float_as_int(lo1.w), count1 = __float_as_int(hi1.w);
+	if (h0 && count0 != 0 && ray_leaf<P>(s, r, ref0, count0)) return kTraceHit;
+	if (h1 && count1 != 0 && ray_leaf<P>(s, r, ref1, count1)) return kTraceHit;
+	const bool in0 = h0 && count0 == 0, in1 = h1 && count1 == 0;
+	if (in0 && in1) {
+		if (r.sp >= kBvhStack) {
+			atomicOr(error, kErrorTraversalLimit);
+			return kTraceMiss;
+		}
+		stack[r.sp++] = ref1;
+		r.node = ref0;
+	} else if (in0 || in1) {
+		r.node = in0 ? ref0 : ref1;
+	} else if (r.sp > 0) {
+		r.node = stack[--r.sp];
+	} else {
+		return kTraceMiss;
+	}
+	return kTraceContinue;
+}
+
+// Any-hit query; true if occluded.
+template <class P> RL_DEV bool any_hit(const SceneView& s, f3 o, f3 d, float t_min, float t_max, uint32_t* error) {
+	TraceRay r;
+	int32_t stack[kBvhStack];
+	int st = trace_begin<P>(s, r, o, d, t_min, t_max);
+	while (st == kTraceContinue) st = trace_step<P>(s, r, stack, error);
+	return st == kTraceHit;
 }
 
 // get_polygon_visibility, shading_pass.frag.glsl:112-129
