@@ -67,14 +67,21 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 		diffuse_weight = mul(diffuse_weight, rop);
 		specular_weight_rgb = mul(specular_weight_rgb, rop);
 	}
-	f3 dir_d = sample_psa<P>(pd, get_noise_2(seed), fa, biased);
-	f3 dir_s = mk3(0.0f, 0.0f, 1.0f);
-	if (ps.psa > 0.0f) {
-		dir_s = sample_psa<P>(ps, get_noise_2(seed), fa, biased);
-		dir_s = normalize<P>(mul(ltc.cosine_to_shading, dir_s));
+	// Both samples come from one copy of the sampling code: the diffuse
+	// sample from pd, then (if the specular polygon has a projected solid
+	// angle) the specular one from ps, in the reference's noise order.
+	f3 dir_d = mk3(0.0f, 0.0f, 1.0f), dir_s = mk3(0.0f, 0.0f, 1.0f);
+#pragma unroll 1
+	for (int j = 0; j != technique_count; ++j) {
+		const f3 dir = sample_psa<P>(j == 0 ? pd : ps, get_noise_2(seed), fa, biased);
+		if (j == 0)
+			dir_d = dir;
+		else
+			dir_s = normalize<P>(mul(ltc.cosine_to_shading, dir));
 	}
 	const bool shadows = pr.shadows && pr.scene.triangle_count != 0;
 	uint32_t modes = 0;
+#pragma unroll 1
 	for (int j = 0; j != technique_count; ++j) {
 		f3 dir = (j == 0) ? dir_d : dir_s;
 		if (dir.z <= 0.0f) continue;
@@ -84,20 +91,23 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 		const bool side = dot(sd.normal, world_dir) > 0.0f;
 		const bool traced = side && shadows;
 		const f3 rb_lit = side ? mul(l.radiance, evaluate_brdf<P>(sd, world_dir)) : splat(0.0f);
+		// This technique's weight and density first, the other's second.
+		const f3 own_weight = j == 0 ? diffuse_weight : specular_weight_rgb;
+		const f3 other_weight = j == 0 ? specular_weight_rgb : diffuse_weight;
+		const float own_density = j == 0 ? diffuse_density : specular_density;
+		const float other_density = j == 0 ? specular_density : diffuse_density;
 		// Outcome 0: visible iff side (unoccluded or untraced); outcome 1:
 		// occluded.
+#pragma unroll 1
 		for (int o = 0; o != (traced ? 2 : 1); ++o) {
 			const bool visibility = (o == 0) ? side : false;
 			f3 integrand = scale(visibility ? rb_lit : splat(0.0f), dir.z);
 			f3 r;
 			if (j == 0 && ps.psa <= 0.0f)
 				r = visibility ? scale(integrand, P::rcp(diffuse_density)) : splat(0.0f);
-			else if (j == 0)
-				r = mis_estimate<P>(pr.mis_heuristic, integrand, diffuse_weight, diffuse_density, specular_weight_rgb,
-				                    specular_density, pr.mis_visibility_estimate);
 			else
-				r = mis_estimate<P>(pr.mis_heuristic, integrand, specular_weight_rgb, specular_density, diffuse_weight,
-				                    diffuse_density, pr.mis_visibility_estimate);
+				r = mis_estimate<P>(pr.mis_heuristic, integrand, own_weight, own_density, other_weight, other_density,
+				                    pr.mis_visibility_estimate);
 			if (j == 0) {
 				if (o == 0) c[0][0] = r; else c[0][1] = r;
 			} else {
@@ -126,7 +136,10 @@ RL_DEV void store_sample(SampleRecord* dst, const f3 (&c)[2][2], float W, uint32
 	q[3] = make_float4(W, __uint_as_float(flags), 0.0f, 0.0f);
 }
 
-template <class P> __global__ void __launch_bounds__(128) ris_sample_kernel(RisParams pr) {
+#ifndef RISLTC_SAMPLE_MIN_BLOCKS
+#define RISLTC_SAMPLE_MIN_BLOCKS 4
+#endif
+template <class P> __global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_kernel(RisParams pr) {
 	const uint32_t np = pr.width * pr.height;
 	ShadeParams sp;  // the fields psa_prepare_both and psa_mis_emit read
 	sp.scene = pr.scene;

@@ -207,7 +207,12 @@ RL_DEV bool psa_prepare_both(const ShadeParams& pr, const ShadingData& sd, Ltc& 
 	const bool fa = pr.fast_atan != 0;
 	side_flip(ltc, sd, l);
 	uint32_t n = l.vertex_count;
+	// One copy of the clipping and preparation code: both polygons are
+	// prepared into ps, the diffuse one moved to pd before the second pass
+	// (as the reference does to keep its code small).
+#pragma unroll 1
 	for (int i = 0; i != 2; ++i) {
+		if (i > 0) pd = ps;
 		mat43 w2l = (i == 0) ? ltc.world_to_shading : mul(ltc.shading_to_cosine, ltc.world_to_shading);
 		f3 verts[kMaxPolygonVertices];
 #pragma unroll
@@ -219,10 +224,7 @@ RL_DEV bool psa_prepare_both(const ShadeParams& pr, const ShadingData& sd, Ltc& 
 			ps.psa = 0.0f;
 			break;
 		}
-		if (i == 0)
-			prepare_psa<P>(pd, vc, verts, fa);
-		else
-			prepare_psa<P>(ps, vc, verts, fa);
+		prepare_psa<P>(ps, vc, verts, fa);
 	}
 	return pd.psa != 0.0f;
 }
