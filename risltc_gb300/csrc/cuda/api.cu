@@ -76,40 +76,72 @@ int grid_for(const risltc_ctx_t* ctx, size_t items) {
 }
 
 // The BVH's device layout for traversal: the root's record {bmin, reference,
-// bmax, triangle count} (8 floats), then one 16-float record per inner node
-// holding both children's records.  A reference is an inner node's record
-// index or a leaf's first triangle; the count is 0 for an inner node.  Inner
-// nodes are numbered depth first, so a left child follows its parent.
-// nodes: risltc_bvh_t's 8-float nodes {bmin, left child or first triangle,
-// bmax, count}, the children of an inner node adjacent.
+// bmax, 0} (8 floats), then one 16-float record per inner node holding both
+// children's records.  A reference is an inner node's record index (>= 0) or
+// a leaf, -(1 + (first triangle << 3 | triangle count)) with 1..7 triangles;
+// a larger leaf becomes a small subtree of leaves of at most 7 triangles, all
+// with the leaf's box, so the triangles tested for a ray do not change.  Inner
+// nodes are numbered depth first.  nodes: risltc_bvh_t's 8-float nodes
+// {bmin, left child or first triangle, bmax, count}, children adjacent.
 std::vector<float> child_pair_nodes(const float* nodes, uint32_t node_count) {
+	(void) node_count;
 	auto word = [&](uint32_t n, int k) {
 		int32_t w;
 		memcpy(&w, nodes + 8 * (size_t) n + k, sizeof(w));
 		return w;
 	};
-	std::vector<int32_t> index(node_count, -1);
-	std::vector<uint32_t> order, stack{0};
-	while (!stack.empty()) {
-		const uint32_t n = stack.back();
-		stack.pop_back();
-		if (word(n, 7) != 0) continue;
-		index[n] = (int32_t) order.size();
-		order.push_back(n);
-		stack.push_back((uint32_t) word(n, 3) + 1);
-		stack.push_back((uint32_t) word(n, 3));
-	}
-	std::vector<float> out(8 + 16 * order.size());
-	auto put = [&](float* dst, uint32_t c) {
-		memcpy(dst, nodes + 8 * (size_t) c, 8 * sizeof(float));
-		const int32_t ref = word(c, 7) == 0 ? index[c] : word(c, 3);
-		memcpy(dst + 3, &ref, sizeof(ref));
+	struct Pending {
+		int32_t record;
+		bool split;          // a range of a large leaf, else an inner node
+		uint32_t node;       // the inner node, or the leaf whose box the range keeps
+		uint32_t first, count;
 	};
-	put(out.data(), 0);
-	for (size_t k = 0; k != order.size(); ++k) {
-		const uint32_t first = (uint32_t) word(order[k], 3);
-		put(out.data() + 8 + 16 * k, first);
-		put(out.data() + 8 + 16 * k + 8, first + 1);
+	std::vector<float> out(8);
+	std::vector<Pending> stack;
+	auto new_record = [&]() {
+		out.resize(out.size() + 16);
+		return (int32_t) ((out.size() - 8) / 16 - 1);
+	};
+	// The reference of a child: node's box and either node itself or the
+	// triangle range [first, first + count) of the leaf node.
+	auto reference = [&](uint32_t node, bool range, uint32_t first, uint32_t count) -> int32_t {
+		if (!range && word(node, 7) == 0) {
+			const int32_t r = new_record();
+			stack.push_back({r, false, node, 0, 0});
+			return r;
+		}
+		if (!range) {
+			first = (uint32_t) word(node, 3);
+			count = (uint32_t) word(node, 7);
+		}
+		if (count <= 7) return -(1 + (int32_t) ((first << 3) | count));
+		const int32_t r = new_record();
+		stack.push_back({r, true, node, first, count});
+		return r;
+	};
+	auto put = [&](size_t at, uint32_t box_node, int32_t ref) {
+		memcpy(out.data() + at, nodes + 8 * (size_t) box_node, 8 * sizeof(float));
+		memcpy(out.data() + at + 3, &ref, sizeof(ref));
+		out[at + 7] = 0.0f;
+	};
+	put(0, 0, reference(0, false, 0, 0));
+	while (!stack.empty()) {
+		const Pending p = stack.back();
+		stack.pop_back();
+		const size_t at = 8 + 16 * (size_t) p.record;
+		if (p.split) {
+			const uint32_t half = p.count / 2;
+			const int32_t r0 = reference(p.node, true, p.first, half);
+			const int32_t r1 = reference(p.node, true, p.first + half, p.count - half);
+			put(at, p.node, r0);
+			put(at + 8, p.node, r1);
+		} else {
+			const uint32_t left = (uint32_t) word(p.node, 3);
+			const int32_t r0 = reference(left, false, 0, 0);
+			const int32_t r1 = reference(left + 1, false, 0, 0);
+			put(at, left, r0);
+			put(at + 8, left + 1, r1);
+		}
 	}
 	return out;
 }
@@ -198,6 +230,8 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	    max_vertex_count < 3 || max_vertex_count > RISLTC_MAX_LIGHT_VERTEX_COUNT || (triangle_count && !triangles))
 		return RISLTC_ERROR_INVALID_ARGUMENT;
 	*out = nullptr;
+	// Leaf references hold the first triangle in 28 bits.
+	if (triangle_count >= (1u << 28)) return RISLTC_ERROR_TOO_LARGE;
 	cudaSetDevice(ctx->device);
 	// Lights: 160-byte records {radiance, vertex_count | plane | 8 x {xyz, 0}}.
 	const size_t stride = 12 + 4 * (size_t) max_vertex_count;

@@ -33,23 +33,26 @@ struct ShadeParams {
 	uint32_t* error;             // error bits (atomicOr)
 };
 
-// Any-hit traversal of the BVH in its child-pair layout (SceneView::pairs):
-// every step loads one inner node with both children's boxes, tests the
-// triangles of the hit leaf children at once and descends into a hit inner
-// child, keeping the other on a stack.  A triangle is tested exactly when
-// every box on its path is hit, so the answer equals a brute-force test of
-// all triangles given conservative boxes; only the order of the tests
-// differs, which an any-hit query does not see.
+// Any-hit traversal of the BVH in its child-pair layout (SceneView::pairs).
+// Each step does one unit of work: test one triangle of the current leaf, or
+// visit one inner node (load both children's boxes, continue with a hit
+// child, keep the other on the stack).  Lanes of a warp thus run the same
+// short step whatever part of the tree they are in.  A triangle is tested
+// exactly when every box on its path is hit, so the answer equals a
+// brute-force test of all triangles given conservative boxes; only the order
+// of the tests differs, which an any-hit query does not see.
 struct TraceRay {
 	f3 o, d;
 	float inv[3];
 	float t_min, t_max;
-	int32_t node;     // the inner node to visit next
+	int32_t node;     // next reference to visit (kNoNode: pop the stack)
+	uint32_t leaf_first, leaf_left;  // triangles of the current leaf still to test
 	int sp;
 	uint32_t visits;
 };
 
 enum : int { kTraceContinue = 0, kTraceMiss = 1, kTraceHit = 2 };
+constexpr int32_t kNoNode = INT32_MIN;
 
 // Slab test of one box against the ray's [t_min, t_max].
 RL_DEV bool ray_box(const TraceRay& r, float4 lo, float4 hi) {
@@ -86,14 +89,7 @@ template <class P> RL_DEV bool ray_triangle(const TraceRay& r, const float4* t) 
 	return tt >= r.t_min && tt <= r.t_max;
 }
 
-template <class P> RL_DEV bool ray_leaf(const SceneView& s, const TraceRay& r, int32_t first, int32_t count) {
-	for (int32_t k = 0; k != count; ++k)
-		if (ray_triangle<P>(r, s.triangles + 3 * (size_t) (first + k))) return true;
-	return false;
-}
-
-// Sets up the ray and tests the root: returns kTraceContinue with r.node set,
-// or the answer when the root is missed or is a leaf.
+// Sets up the ray and tests the root box: kTraceMiss, or kTraceContinue.
 template <class P> RL_DEV int trace_begin(const SceneView& s, TraceRay& r, f3 o, f3 d, float t_min, float t_max) {
 	r.o = o;
 	r.d = d;
@@ -104,43 +100,54 @@ template <class P> RL_DEV int trace_begin(const SceneView& s, TraceRay& r, f3 o,
 	r.t_max = t_max;
 	r.sp = 0;
 	r.visits = 0;
+	r.leaf_left = 0;
+	r.leaf_first = 0;
 	if (s.triangle_count == 0) return kTraceMiss;
 	const float4 lo = __ldg(s.pairs), hi = __ldg(s.pairs + 1);
 	if (!ray_box(r, lo, hi)) return kTraceMiss;
-	const int32_t ref = __float_as_int(lo.w), count = __float_as_int(hi.w);
-	if (count != 0) return ray_leaf<P>(s, r, ref, count) ? kTraceHit : kTraceMiss;
-	r.node = ref;
+	r.node = __float_as_int(lo.w);
 	return kTraceContinue;
 }
 
-// One inner node.  Gives up after kTraversalLimit steps or on a stack
-// overflow, records the error and reports "not occluded".
+// One step.  Gives up after kTraversalLimit steps or on a stack overflow,
+// records the error and reports "not occluded".
 template <class P> RL_DEV int trace_step(const SceneView& s, TraceRay& r, int32_t* stack, uint32_t* error) {
 	if (++r.visits > kTraversalLimit) {
 		atomicOr(error, kErrorTraversalLimit);
 		return kTraceMiss;
 	}
+	if (r.leaf_left != 0) {
+		const bool hit = ray_triangle<P>(r, s.triangles + 3 * (size_t) r.leaf_first);
+		++r.leaf_first;
+		--r.leaf_left;
+		return hit ? kTraceHit : kTraceContinue;
+	}
+	if (r.node == kNoNode) {
+		if (r.sp == 0) return kTraceMiss;
+		r.node = stack[--r.sp];
+	}
+	if (r.node < 0) {
+		const uint32_t code = (uint32_t) (-(r.node + 1));
+		r.leaf_first = code >> 3;
+		r.leaf_left = code & 7u;
+		r.node = kNoNode;
+		return kTraceContinue;
+	}
 	const float4* n = s.pairs + 2 + 4 * (size_t) r.node;
 	const float4 lo0 = __ldg(n), hi0 = __ldg(n + 1), lo1 = __ldg(n + 2), hi1 = __ldg(n + 3);
 	const bool h0 = ray_box(r, lo0, hi0), h1 = ray_box(r, lo1, hi1);
-	const int32_t ref0 = __float_as_int(lo0.w), count0 = __float_as_int(hi0.w);
-	const int32_t ref1 = __float_as_int(lo1.w), count1 = __float_as_int(hi1.w);
-	if (h0 && count0 != 0 && ray_leaf<P>(s, r, ref0, count0)) return kTraceHit;
-	if (h1 && count1 != 0 && ray_leaf<P>(s, r, ref1, count1)) return kTraceHit;
-	const bool in0 = h0 && count0 == 0, in1 = h1 && count1 == 0;
-	if (in0 && in1) {
+	const int32_t ref0 = __float_as_int(lo0.w), ref1 = __float_as_int(lo1.w);
+	if (h0 && h1) {
 		if (r.sp >= kBvhStack) {
 			atomicOr(error, kErrorTraversalLimit);
 			return kTraceMiss;
 		}
-		stack[r.sp++] = ref1;
-		r.node = ref0;
-	} else if (in0 || in1) {
-		r.node = in0 ? ref0 : ref1;
-	} else if (r.sp > 0) {
-		r.node = stack[--r.sp];
+		// Leaves first: their triangles may end the query early.
+		const bool leaf1_first = ref1 < 0 && ref0 >= 0;
+		stack[r.sp++] = leaf1_first ? ref0 : ref1;
+		r.node = leaf1_first ? ref1 : ref0;
 	} else {
-		return kTraceMiss;
+		r.node = h0 ? ref0 : (h1 ? ref1 : kNoNode);
 	}
 	return kTraceContinue;
 }
