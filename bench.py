@@ -13,6 +13,7 @@ Prints one JSON line (rank 0).  N > 1 runs one process per GPU (torchrun),
 each shading its own frame (weak scaling, no data-path collective).
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -25,8 +26,10 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-WORKLOAD = "shadowed single frame: 1920x1080 fBm heightfield, 1024 polygon lights (3-8 vertices), " \
-           "200k occluder triangles (SAH BVH), plain LTC-RIS M=32, 4 spp"
+def workload_name(a):
+    return ("shadowed single frame: %dx%d fBm heightfield, %d polygon lights (3-8 vertices), %dk occluder "
+            "triangles (SAH BVH), plain LTC-RIS M=%d, %d spp" % (a.width, a.height, a.lights, a.triangles // 1000,
+                                                                 a.candidates, a.spp))
 METRIC = "Gsamples/s (plain LTC-RIS, shadowed 1080p frame, 1024 lights, M=32, 4 spp)"
 L2_BYTES = 129 * 1024 * 1024
 
@@ -34,7 +37,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--width", type=int, default=1920)
@@ -58,22 +61,31 @@ def make_workload(a, seed=0):
 
 # ----------------------------------------------------------------- clocks --
 class ClockSampler:
-    """nvidia-smi clock and throttle-reason samples during the timed region."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clock and throttle-reason samples (every 50 ms, started
+    before the warm-up so that it is running when the timed region begins);
+    stop() keeps the samples taken between mark_start() and mark_stop()."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device_index=0):
         self.proc = None
+        self.t0 = self.t1 = None
         self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(device_index), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_stop(self):
+        self.t1 = time.time()
 
     def stop(self):
         if self.proc is None:
@@ -85,18 +97,39 @@ class ClockSampler:
         with open(self.path) as f:
             for line in f:
                 parts = [x.strip() for x in line.split(",")]
-                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
-                    rows.append(parts)
+                if len(parts) < 10 or not parts[2].replace(".", "").isdigit():
+                    continue
+                try:
+                    ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                except ValueError:
+                    ts = None
+                rows.append((ts, parts[1:]))
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(r[1]) for r in rows]
-        smax = max(float(r[2]) for r in rows)
-        power = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        window = [r for ts, r in rows if ts is not None and self.t0 is not None and self.t0 <= ts <= self.t1]
+        note = "samples inside the timed region"
+        if not window:
+            window = [r for _, r in rows]
+            note = "no sample fell inside the timed region: all samples of the run"
+        sm = [float(r[1]) for r in window]
+        smax = max(float(r[2]) for r in window)
+        power = [float(r[3]) for r in window if r[3].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
-        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
-        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax, "reasons": reasons,
-                "samples": len(rows), "power_w_max": max(power) if power else None}
+        reasons = sorted({names[k] for r in window for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": reasons, "samples": len(window),
+                "power_w_max": max(power) if power else None, "note": note}
+
+
+def measured_traffic(kernel, samples_per_step):
+    """DRAM bytes (read + write) per launch of `kernel` for this step, from the
+    ncu capture summarised in profiles/traffic.json, scaled from the captured
+    launch's pixel-samples to this step's (the traffic grows with them)."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            t = json.load(f)[kernel]
+        return t["dram_bytes"] * samples_per_step / t["pixel_samples"], t["source"]
+    except (OSError, ValueError, KeyError):
+        return None, None
 
 
 def measured_peaks():
@@ -174,7 +207,7 @@ def run_reference(a, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gsamples/s", "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * info["seconds"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": "%d pixels drawn uniformly from the frame, 1 spp" % (
+        "config": {"workload": workload_name(a), "sample": "%d pixels drawn uniformly from the frame, 1 spp" % (
             info["samples"])},
         "cpu_baseline": {"value": value, "unit": "Gsamples/s", "cores": info["threads"], "kind": "port",
                          "sample": "%d pixel-samples drawn uniformly from the frame per step, FP32 oracle "
@@ -204,23 +237,27 @@ def run_ours(a, rank, world, local_rank):
     out = torch.empty((P, 3), dtype=torch.float32, device="cuda")
     # Each rank shades different frames (its own noise seeds).
     seed = rank * 1_000_000
+    clocks = ClockSampler(local_rank) if rank == 0 else None
     for _ in range(a.warmup):
         seed = rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, out_rgb=out,
                         primitive=prim)
     ctx.check()
-    clocks = ClockSampler(local_rank) if rank == 0 else None
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ctx.profile(True)  # per-kernel CUDA events on the same stream
+    if clocks:
+        clocks.mark_start()
     start.record(stream)
     for _ in range(a.steps):
         seed = rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, out_rgb=out,
                         primitive=prim)
     stop.record(stream)
     torch.cuda.synchronize()
+    if clocks:
+        clocks.mark_stop()
     if dist:
         dist.barrier()
     clock_info = clocks.stop() if clocks else None
@@ -296,12 +333,12 @@ def run_ours(a, rank, world, local_rank):
     calls = max(prof["calls"], 1)
     # One launch of each kernel per step (all spp frames in one call).  The
     # resolve kernel's few operations are counted with the sample kernel.
-    kernels = {"ris_candidates_kernel": {"ms_per_launch": prof["candidates"] / calls},
+    kernels = {"ris_candidates_binned_kernel": {"ms_per_launch": prof["candidates"] / calls},
                "ris_sample_kernel": {"ms_per_launch": prof["shade"] / calls},
                "shadow_trace_kernel": {"ms_per_launch": prof["shadow_trace"] / calls},
                "ris_resolve_kernel": {"ms_per_launch": prof["resolve"] / calls}}
     if flops_per_sample:
-        kernels["ris_candidates_kernel"]["flops_per_sample"] = info["candidate_flops_per_sample"]
+        kernels["ris_candidates_binned_kernel"]["flops_per_sample"] = info["candidate_flops_per_sample"]
         kernels["ris_sample_kernel"]["flops_per_sample"] = info["shade_flops_per_sample"]
         kernels["shadow_trace_kernel"]["flops_per_sample"] = info["trace_flops_per_sample"]
         kernels["ris_resolve_kernel"]["flops_per_sample"] = 0.0
@@ -311,8 +348,9 @@ def run_ours(a, rank, world, local_rank):
             k["frac"] = k["achieved_tflops"] / fp32_peak
         dominant = max(kernels, key=lambda k: kernels[k]["ms_per_launch"])
         d = kernels[dominant]
+        traffic, traffic_source = measured_traffic(dominant, samples_per_step)
         roofline = {"bound": "fp32", "achieved": d["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
-                    "frac": d["frac"], "traffic": None, "kernel": dominant,
+                    "frac": d["frac"], "traffic": traffic, "traffic_source": traffic_source, "kernel": dominant,
                     "flops_per_sample": d["flops_per_sample"],
                     "whole_step_frac": flops_per_sample * samples_per_step / (elapsed / a.steps) / 1e12 / fp32_peak,
                     "peak_source": "derived: 2 x 128 FP32 lanes x %d SMs x %.0f MHz (max SM clock of "
@@ -321,10 +359,11 @@ def run_ours(a, rank, world, local_rank):
         "metric": METRIC, "value": result["value"], "unit": "Gsamples/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": result["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "width": hs.width, "height": hs.height, "lights": hs.light_count,
+        "config": {"workload": workload_name(a), "width": hs.width, "height": hs.height, "lights": hs.light_count,
                    "triangles": int(hs.triangles.shape[0]), "candidates": a.candidates, "spp": a.spp,
                    "numerics": a.numerics, "samples_per_step": samples_per_step,
-                   "l2": "inputs larger than L2 (G-buffer %.0f MB > 129 MB)" % (hs.gbuffer.nbytes / 1e6),
+                   "l2": ("inputs larger than L2 (G-buffer %.0f MB > 129 MB)" if hs.gbuffer.nbytes > L2_BYTES else
+                          "inputs smaller than L2 (G-buffer %.0f MB < 129 MB), no flush") % (hs.gbuffer.nbytes / 1e6),
                    "parallelism": "one frame per GPU" if world > 1 else "single GPU"},
         "gpu_launches": 4 * a.steps,
         "kernels": kernels,

@@ -271,7 +271,8 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx);
 /* Uploads lights (the std140 buffer of risltc_write_lights), the LTC table
    and, if triangle_count > 0, builds and uploads the BVH of the occluders
    (9 floats per triangle; fewer than 2^28 triangles, else
-   RISLTC_ERROR_TOO_LARGE).  All inputs are host memory. */
+   RISLTC_ERROR_TOO_LARGE; all finite, else RISLTC_ERROR_NON_FINITE).  All
+   inputs are host memory. */
 EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, uint32_t light_count,
                                  uint32_t max_vertex_count, const risltc_ltc_table_t* ltc, const float* triangles,
                                  uint32_t triangle_count, risltc_scene_t** scene);

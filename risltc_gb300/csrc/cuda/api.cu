@@ -1,5 +1,6 @@
 // api.cu - the device half of the C ABI in include/risltc.h: contexts,
 // scene upload, frame shading and shadow queries.
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -232,6 +233,9 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	*out = nullptr;
 	// Leaf references hold the first triangle in 28 bits.
 	if (triangle_count >= (1u << 28)) return RISLTC_ERROR_TOO_LARGE;
+	// Finite occluders keep the traversal's box tests free of NaN.
+	for (size_t i = 0; i != 9 * (size_t) triangle_count; ++i)
+		if (!std::isfinite(triangles[i])) return RISLTC_ERROR_NON_FINITE;
 	cudaSetDevice(ctx->device);
 	// Lights: 160-byte records {radiance, vertex_count | plane | 8 x {xyz, 0}}.
 	const size_t stride = 12 + 4 * (size_t) max_vertex_count;

@@ -49,24 +49,41 @@ struct TraceRay {
 	uint32_t leaf_first, leaf_left;  // triangles of the current leaf still to test
 	int sp;
 	uint32_t visits;
+	bool minmax;      // no slab product can be NaN: the min/max form applies
 };
 
 enum : int { kTraceContinue = 0, kTraceMiss = 1, kTraceHit = 2 };
 constexpr int32_t kNoNode = INT32_MIN;
 
-// Slab test of one box against the ray's [t_min, t_max].
-RL_DEV bool ray_box(const TraceRay& r, float4 lo, float4 hi) {
+// Slab test of one box against the ray's [t_min, t_max]; *entry gets the
+// entry distance.  Per axis t0 = (bmin - o) * inv, t1 = (bmax - o) * inv;
+// the interval is narrowed by min(t0, t1) and max(t0, t1), an endpoint that
+// is NaN leaving its side unchanged.  When no product can be NaN (finite box
+// and origin, finite non-zero inv) the same result comes from IEEE min/max
+// instructions, used then.
+RL_DEV bool ray_box(const TraceRay& r, float4 lo, float4 hi, float* entry) {
 	const float bmin[3] = {lo.x, lo.y, lo.z}, bmax[3] = {hi.x, hi.y, hi.z};
 	const float org[3] = {r.o.x, r.o.y, r.o.z};
 	float t0s = r.t_min, t1s = r.t_max;
+	if (r.minmax) {
 #pragma unroll
-	for (int ax = 0; ax != 3; ++ax) {
-		float t0 = (bmin[ax] - org[ax]) * r.inv[ax];
-		float t1 = (bmax[ax] - org[ax]) * r.inv[ax];
-		float tn = t0 < t1 ? t0 : t1, tf = t0 < t1 ? t1 : t0;
-		if (tn == tn && tn > t0s) t0s = tn;
-		if (tf == tf && tf < t1s) t1s = tf;
+		for (int ax = 0; ax != 3; ++ax) {
+			const float t0 = (bmin[ax] - org[ax]) * r.inv[ax];
+			const float t1 = (bmax[ax] - org[ax]) * r.inv[ax];
+			t0s = fmaxf(t0s, fminf(t0, t1));
+			t1s = fminf(t1s, fmaxf(t0, t1));
+		}
+	} else {
+#pragma unroll
+		for (int ax = 0; ax != 3; ++ax) {
+			const float t0 = (bmin[ax] - org[ax]) * r.inv[ax];
+			const float t1 = (bmax[ax] - org[ax]) * r.inv[ax];
+			const float tn = t0 < t1 ? t0 : t1, tf = t0 < t1 ? t1 : t0;
+			if (tn == tn && tn > t0s) t0s = tn;
+			if (tf == tf && tf < t1s) t1s = tf;
+		}
 	}
+	*entry = t0s;
 	return t0s <= t1s;
 }
 
@@ -102,9 +119,18 @@ template <class P> RL_DEV int trace_begin(const SceneView& s, TraceRay& r, f3 o,
 	r.visits = 0;
 	r.leaf_left = 0;
 	r.leaf_first = 0;
+	// Boxes are finite (the scene rejects non-finite triangles); with a
+	// finite origin and finite non-zero inv no slab product is NaN, and with
+	// t_min and t_max not NaN neither is an interval end.
+	r.minmax = !isnan(t_min) && !isnan(t_max);
+	const float oc[3] = {o.x, o.y, o.z};
+#pragma unroll
+	for (int ax = 0; ax != 3; ++ax)
+		r.minmax = r.minmax && isfinite(oc[ax]) && isfinite(r.inv[ax]) && r.inv[ax] != 0.0f;
 	if (s.triangle_count == 0) return kTraceMiss;
 	const float4 lo = __ldg(s.pairs), hi = __ldg(s.pairs + 1);
-	if (!ray_box(r, lo, hi)) return kTraceMiss;
+	float entry;
+	if (!ray_box(r, lo, hi, &entry)) return kTraceMiss;
 	r.node = __float_as_int(lo.w);
 	return kTraceContinue;
 }
@@ -135,17 +161,19 @@ template <class P> RL_DEV int trace_step(const SceneView& s, TraceRay& r, int32_
 	}
 	const float4* n = s.pairs + 2 + 4 * (size_t) r.node;
 	const float4 lo0 = __ldg(n), hi0 = __ldg(n + 1), lo1 = __ldg(n + 2), hi1 = __ldg(n + 3);
-	const bool h0 = ray_box(r, lo0, hi0), h1 = ray_box(r, lo1, hi1);
+	float e0, e1;
+	const bool h0 = ray_box(r, lo0, hi0, &e0), h1 = ray_box(r, lo1, hi1, &e1);
 	const int32_t ref0 = __float_as_int(lo0.w), ref1 = __float_as_int(lo1.w);
 	if (h0 && h1) {
 		if (r.sp >= kBvhStack) {
 			atomicOr(error, kErrorTraversalLimit);
 			return kTraceMiss;
 		}
-		// Leaves first: their triangles may end the query early.
-		const bool leaf1_first = ref1 < 0 && ref0 >= 0;
-		stack[r.sp++] = leaf1_first ? ref0 : ref1;
-		r.node = leaf1_first ? ref1 : ref0;
+		// The nearer child first: an occluder near the origin ends the
+		// query early.
+		const bool second_first = e1 < e0;
+		stack[r.sp++] = second_first ? ref0 : ref1;
+		r.node = second_first ? ref1 : ref0;
 	} else {
 		r.node = h0 ? ref0 : (h1 ? ref1 : kNoNode);
 	}
