@@ -44,6 +44,7 @@ struct WarpTile {
 	uint16_t item_slot[kItems];  // pixel lane * kChunk + candidate of the chunk
 	uint16_t deferred[kItems];
 	float p_hat[kItems];         // [pixel lane][candidate of the chunk]
+	int32_t slot_light[kItems];  // [pixel lane][candidate of the chunk]
 	uint32_t deferred_count;
 };
 
@@ -94,13 +95,16 @@ __device__ __noinline__ float clipped_integral(mat43 t, const float4* record, ui
 
 // One candidate (ltc_cp_candidate, then p_hat = length(color)) with the
 // frame in shared memory.  The two LTC integrals run in one loop over the
-// spaces, and each polygon is streamed vertex by vertex from the light
-// record: a first pass counts the vertices above the horizon, a second
-// transforms, normalises and integrates edge after edge in the order of
-// calculate_ltc (edges 0-1, ..., (n-2)-(n-1), then (n-1)-0).  The code stays
-// small and the vertex count of a sorted group is uniform across the warp.
-// With allow_clip false, returns false as soon as a space clips the polygon
-// partially; the caller defers the item.
+// spaces.  Each polygon streams vertex by vertex from the light record (the
+// next vertex's load issued before the current one is used): every vertex is
+// transformed, counted if above the horizon, normalised and joined to the
+// previous one in the edge order of calculate_ltc (edges 0-1, ...,
+// (n-2)-(n-1), then (n-1)-0).  The sum is kept when the whole polygon is
+// above the horizon (the common case); a polygon entirely below contributes
+// nothing, and a partially clipped one goes through clip_polygon instead.
+// The code stays small and the vertex count of a sorted group is uniform
+// across the warp.  With allow_clip false, returns false as soon as a space
+// clips the polygon partially; the caller defers the item.
 template <class P>
 RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
 	const float4 head = __ldg(record), pl = __ldg(record + 1);
@@ -116,25 +120,33 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 #pragma unroll
 		for (int c = 0; c != 4; ++c) t.c[c] = mk3(m[3 * c], m[3 * c + 1], m[3 * c + 2]);
 		const bool negate_y = s == 0 && flip;
-		uint32_t above = 0;
-#pragma unroll 1
-		for (uint32_t j = 0; j != n; ++j) above += local_vertex(t, record, j, negate_y).z > 0.0f ? 1u : 0u;
-		const bool partial = above != 0 && above != n;
-		if (partial && !allow_clip) return false;
+		float4 q = __ldg(record + 2);
+		f3 v = mul_point(t, mk3(q.x, q.y, q.z));
+		v.y = negate_y ? -v.y : v.y;
+		q = __ldg(record + 3);
+		uint32_t above = v.z > 0.0f ? 1u : 0u;
+		const f3 first = normalize<P>(v);
+		f3 prev = first;
 		float r = 0.0f;
-		bool a = above == 0;
-		if (above == n) {
-			const f3 first = normalize<P>(local_vertex(t, record, 0, negate_y));
-			f3 prev = first;
 #pragma unroll 1
-			for (uint32_t j = 1; j != n; ++j) {
-				const f3 cur = normalize<P>(local_vertex(t, record, j, negate_y));
-				r += integrate_edge<P>(prev, cur);
-				prev = cur;
-			}
-			r += integrate_edge<P>(prev, first);
+		for (uint32_t j = 1; j != n; ++j) {
+			v = mul_point(t, mk3(q.x, q.y, q.z));
+			v.y = negate_y ? -v.y : v.y;
+			q = __ldg(record + 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
+			above += v.z > 0.0f ? 1u : 0u;
+			const f3 cur = normalize<P>(v);
+			r += integrate_edge<P>(prev, cur);
+			prev = cur;
+		}
+		r += integrate_edge<P>(prev, first);
+		bool a = false;
+		if (above == n) {
 			r = fabsf(r);
-		} else if (partial) {
+		} else if (above == 0) {
+			r = 0.0f;
+			a = true;
+		} else {
+			if (!allow_clip) return false;
 			r = clipped_integral<P>(t, record, n, negate_y);
 			a = r < 0.0f;
 			r = a ? 0.0f : r;
@@ -220,6 +232,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 						idx = idx > n_lights - 1 ? n_lights - 1 : idx;
 						get_noise_1(draw);
 						light[k] = idx;
+						tile.slot_light[lane * kChunk + k] = idx;
 						bin[k] = __float_as_uint(__ldg(light_record(pr.scene, idx)).w) - 3u;
 						counts += 1ull << (10 * bin[k]);
 					}
@@ -293,7 +306,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 							const float w = P::div(p_hat, p);
 							w_sum += w;
 							if (w > 0.0f && rnd < P::div(w, w_sum)) {
-								res_index = light[k];
+								res_index = tile.slot_light[lane * kChunk + k];
 								sample_value = p_hat;
 							}
 						}
