@@ -1,8 +1,8 @@
 // ris_binned.cuh - the RIS candidate phase as a warp-per-tile kernel with
 // work binning.
 //
-// Each warp owns 32 consecutive pixels.  Per chunk of kChunk candidates the
-// warp
+// Each warp owns 32 consecutive pixels and takes their candidates in
+// super-chunks of kSuper, each made of chunks of kChunk.  Per chunk the warp
 //   1. draws every pixel's candidate lights from that pixel's noise stream
 //      (the LCG sequence of shading_pass.frag.glsl:728-736: a light draw, then
 //      the reservoir draw, per candidate);
@@ -11,9 +11,12 @@
 //      mostly evaluate polygons with the same number of vertices;
 //   3. evaluates the items with each pixel's LTC frame read from shared
 //      memory; an item whose polygon is partially clipped in either space is
-//      deferred, and the warp evaluates the deferred items together;
-//   4. lets each lane replay its pixel's reservoir updates in candidate order
-//      (insert_in_reservoir, reservoir.glsl:34-41).
+//      deferred to a list that the warp evaluates 32 at a time, so the slow
+//      clipping path runs with full warps.
+// At the end of the super-chunk the last deferred items are evaluated and
+//   4. each lane replays its pixel's reservoir updates in candidate order
+//      (insert_in_reservoir, reservoir.glsl:34-41), drawing the same noise
+//      again.
 // Every p_hat is computed by the same operations on the same values as in
 // ris_candidates_kernel and the reservoir sees them in the same order, so the
 // reservoir records are bit-identical.
@@ -33,18 +36,29 @@ namespace risltc {
 #endif
 constexpr int kChunk = RISLTC_BINNED_CHUNK;  // candidates per pixel per chunk
 constexpr int kItems = 32 * kChunk;          // items per warp per chunk
+constexpr int kDeferred = kItems + 32;       // deferred items pending at most
+
+// Candidates per pixel per super-chunk (measured best: 32 in exact numerics,
+// 16 in fast numerics, where the smaller tile leaves more L1 for the lights).
+template <class P> struct BinnedSuper {
+	static constexpr int value = 32;
+};
+template <> struct BinnedSuper<FastNumerics> {
+	static constexpr int value = 16;
+};
 constexpr int kFrameWords = 45;              // 44 used; odd stride avoids bank conflicts
 constexpr int kBinnedWarps = 4;              // warps per block
 constexpr int kBins = kMaxLightVertices - 2; // vertex counts 3..8
 static_assert(kItems < 1024, "10-bit bin counters");
 
-struct WarpTile {
+template <int kSuper> struct WarpTile {
+	static_assert(kSuper % kChunk == 0 && 32 * kSuper <= 65536, "super-chunk layout");
 	float frame[32][kFrameWords];
 	int32_t item_light[kItems];
-	uint16_t item_slot[kItems];  // pixel lane * kChunk + candidate of the chunk
-	uint16_t deferred[kItems];
-	float p_hat[kItems];         // [pixel lane][candidate of the chunk]
-	int32_t slot_light[kItems];  // [pixel lane][candidate of the chunk]
+	uint16_t item_slot[kItems];  // pixel lane * kSuper + candidate of the super-chunk
+	float p_hat[32 * kSuper];    // [pixel lane][candidate of the super-chunk]
+	int32_t deferred_light[kDeferred];
+	uint16_t deferred_slot[kDeferred];
 	uint32_t deferred_count;
 };
 
@@ -173,7 +187,8 @@ template <class P>
 __global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
 ris_candidates_binned_kernel(RisParams pr) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	WarpTile& tile = reinterpret_cast<WarpTile*>(smem_raw)[threadIdx.x / 32];
+	constexpr int kSuper = BinnedSuper<P>::value;
+	WarpTile<kSuper>& tile = reinterpret_cast<WarpTile<kSuper>*>(smem_raw)[threadIdx.x / 32];
 	const uint32_t lane = threadIdx.x % 32;
 	const uint32_t np = pr.width * pr.height;
 	const int n_lights = pr.scene.light_count;
@@ -215,100 +230,117 @@ ris_candidates_binned_kernel(RisParams pr) {
 			}
 			float w_sum = 0.0f, sample_value = 0.0f;
 			int res_index = -1;
-			for (int c0 = 0; c0 < pr.candidate_count; c0 += kChunk) {
-				const int chunk = min(kChunk, pr.candidate_count - c0);
-				// 1. This lane's candidate lights; bin them by vertex count
-				//    (six 10-bit counters).
-				int light[kChunk];
-				uint32_t bin[kChunk];
+			for (int cs = 0; cs < pr.candidate_count; cs += kSuper) {
+				const int super_count = min(kSuper, pr.candidate_count - cs);
 				uint32_t draw = seed;
-				unsigned long long counts = 0;
-#pragma unroll
-				for (int k = 0; k != kChunk; ++k) {
-					light[k] = -1;
-					bin[k] = kBins;
-					if (valid && k < chunk) {
-						int idx = (int) (get_noise_1(draw) * (float) n_lights);
-						idx = idx > n_lights - 1 ? n_lights - 1 : idx;
-						get_noise_1(draw);
-						light[k] = idx;
-						tile.slot_light[lane * kChunk + k] = idx;
-						bin[k] = __float_as_uint(__ldg(light_record(pr.scene, idx)).w) - 3u;
-						counts += 1ull << (10 * bin[k]);
-					}
-				}
-				// 2. Counting sort: exclusive scan of the counters across the
-				//    warp, then each bin's start.
-				unsigned long long prefix = counts;
-#pragma unroll
-				for (int d = 1; d < 32; d <<= 1) {
-					const unsigned long long o = __shfl_up_sync(0xffffffffu, prefix, d);
-					if ((int) lane >= d) prefix += o;
-				}
-				const unsigned long long totals = __shfl_sync(0xffffffffu, prefix, 31);
-				prefix -= counts;
-				uint32_t start[kBins + 1];
-				start[0] = 0;
-#pragma unroll
-				for (int b = 0; b != kBins; ++b) start[b + 1] = start[b] + (uint32_t) ((totals >> (10 * b)) & 1023u);
-				const uint32_t item_count = start[kBins];
-#pragma unroll
-				for (int k = 0; k != kChunk; ++k) {
-					if (bin[k] < kBins) {
-						const uint32_t b = bin[k];
-						uint32_t s = 0;
-#pragma unroll
-						for (int q = 0; q != kBins; ++q)
-							if (q == (int) b) s = start[q];
-						const uint32_t pos = s + (uint32_t) ((prefix >> (10 * b)) & 1023u);
-						prefix += 1ull << (10 * b);
-						tile.item_light[pos] = light[k];
-						tile.item_slot[pos] = (uint16_t) (lane * kChunk + k);
-					}
-				}
 				if (lane == 0) tile.deferred_count = 0;
 				__syncwarp();
-				// 3. Evaluate the sorted items, 32 at a time; defer partial clips.
-				for (uint32_t base = 0; base < item_count; base += 32) {
-					const uint32_t it = base + lane;
-					if (it < item_count) {
-						const uint32_t slot = tile.item_slot[it];
-						float ph;
-						if (binned_candidate<P>(tile.frame[slot / kChunk], light_record(pr.scene, tile.item_light[it]),
-						                        false, ph))
-							tile.p_hat[slot] = ph;
-						else
-							tile.deferred[atomicAdd(&tile.deferred_count, 1u)] = (uint16_t) it;
-					}
-				}
-				__syncwarp();
-				const uint32_t deferred = tile.deferred_count;
-				for (uint32_t base = 0; base < deferred; base += 32) {
-					const uint32_t d = base + lane;
-					if (d < deferred) {
-						const uint32_t it = tile.deferred[d];
-						const uint32_t slot = tile.item_slot[it];
-						float ph = 0.0f;
-						binned_candidate<P>(tile.frame[slot / kChunk], light_record(pr.scene, tile.item_light[it]), true,
-						                    ph);
-						tile.p_hat[slot] = ph;
-					}
-				}
-				__syncwarp();
-				// 4. Reservoir updates in candidate order.
-				if (valid) {
+				for (int c0 = 0; c0 < super_count; c0 += kChunk) {
+					const int chunk = min(kChunk, super_count - c0);
+					// 1. This lane's candidate lights; bin them by vertex count
+					//    (six 10-bit counters).
+					int light[kChunk];
+					uint32_t bin[kChunk];
+					unsigned long long counts = 0;
 #pragma unroll
 					for (int k = 0; k != kChunk; ++k) {
-						if (k < chunk) {
-							get_noise_1(seed);
-							const float rnd = get_noise_1(seed);
-							const float p_hat = tile.p_hat[lane * kChunk + k];
-							const float w = P::div(p_hat, p);
-							w_sum += w;
-							if (w > 0.0f && rnd < P::div(w, w_sum)) {
-								res_index = tile.slot_light[lane * kChunk + k];
-								sample_value = p_hat;
+						light[k] = -1;
+						bin[k] = kBins;
+						if (valid && k < chunk) {
+							int idx = (int) (get_noise_1(draw) * (float) n_lights);
+							idx = idx > n_lights - 1 ? n_lights - 1 : idx;
+							get_noise_1(draw);
+							light[k] = idx;
+							bin[k] = __float_as_uint(__ldg(light_record(pr.scene, idx)).w) - 3u;
+							counts += 1ull << (10 * bin[k]);
+						}
+					}
+					// 2. Counting sort: exclusive scan of the counters across
+					//    the warp, then each bin's start.
+					unsigned long long prefix = counts;
+#pragma unroll
+					for (int d = 1; d < 32; d <<= 1) {
+						const unsigned long long o = __shfl_up_sync(0xffffffffu, prefix, d);
+						if ((int) lane >= d) prefix += o;
+					}
+					const unsigned long long totals = __shfl_sync(0xffffffffu, prefix, 31);
+					prefix -= counts;
+					uint32_t start[kBins + 1];
+					start[0] = 0;
+#pragma unroll
+					for (int b = 0; b != kBins; ++b)
+						start[b + 1] = start[b] + (uint32_t) ((totals >> (10 * b)) & 1023u);
+					const uint32_t item_count = start[kBins];
+#pragma unroll
+					for (int k = 0; k != kChunk; ++k) {
+						if (bin[k] < kBins) {
+							const uint32_t b = bin[k];
+							uint32_t s = 0;
+#pragma unroll
+							for (int q = 0; q != kBins; ++q)
+								if (q == (int) b) s = start[q];
+							const uint32_t pos = s + (uint32_t) ((prefix >> (10 * b)) & 1023u);
+							prefix += 1ull << (10 * b);
+							tile.item_light[pos] = light[k];
+							tile.item_slot[pos] = (uint16_t) (lane * kSuper + c0 + k);
+						}
+					}
+					__syncwarp();
+					// 3. Evaluate the sorted items, 32 at a time; defer partial
+					//    clips, and evaluate deferred items whenever 32 are
+					//    pending.
+					for (uint32_t base = 0; base < item_count; base += 32) {
+						const uint32_t it = base + lane;
+						if (it < item_count) {
+							const uint32_t slot = tile.item_slot[it];
+							const int32_t l = tile.item_light[it];
+							float ph;
+							if (binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph)) {
+								tile.p_hat[slot] = ph;
+							} else {
+								const uint32_t d = atomicAdd(&tile.deferred_count, 1u);
+								tile.deferred_light[d] = l;
+								tile.deferred_slot[d] = (uint16_t) slot;
 							}
+						}
+					}
+					__syncwarp();
+					for (uint32_t pending = tile.deferred_count; pending >= 32; pending -= 32) {
+						const uint32_t d = pending - 32 + lane;
+						const uint32_t slot = tile.deferred_slot[d];
+						float ph = 0.0f;
+						binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, tile.deferred_light[d]),
+						                    true, ph);
+						tile.p_hat[slot] = ph;
+						__syncwarp();
+						if (lane == 0) tile.deferred_count = pending - 32;
+						__syncwarp();
+					}
+				}
+				// The rest of the deferred items.
+				const uint32_t rest = tile.deferred_count;
+				if (lane < rest) {
+					const uint32_t slot = tile.deferred_slot[lane];
+					float ph = 0.0f;
+					binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, tile.deferred_light[lane]),
+					                    true, ph);
+					tile.p_hat[slot] = ph;
+				}
+				__syncwarp();
+				// 4. Reservoir updates in candidate order, drawing the same
+				//    noise again.
+				if (valid) {
+#pragma unroll 4
+					for (int k = 0; k < super_count; ++k) {
+						int idx = (int) (get_noise_1(seed) * (float) n_lights);
+						idx = idx > n_lights - 1 ? n_lights - 1 : idx;
+						const float rnd = get_noise_1(seed);
+						const float p_hat = tile.p_hat[lane * kSuper + k];
+						const float w = P::div(p_hat, p);
+						w_sum += w;
+						if (w > 0.0f && rnd < P::div(w, w_sum)) {
+							res_index = idx;
+							sample_value = p_hat;
 						}
 					}
 				}
@@ -323,6 +355,18 @@ ris_candidates_binned_kernel(RisParams pr) {
 	}
 }
 
-inline constexpr size_t binned_smem_bytes() { return sizeof(WarpTile) * kBinnedWarps; }
+template <class P> constexpr size_t binned_smem_bytes() {
+	return sizeof(WarpTile<BinnedSuper<P>::value>) * kBinnedWarps;
+}
+
+// Launches the binned candidate kernel; its shared memory exceeds the 48 KB
+// available without opting in, so the limit is raised first (per device).
+template <class P> cudaError_t launch_candidates_binned(const RisParams& p, cudaStream_t stream, int grid) {
+	cudaError_t e = cudaFuncSetAttribute(ris_candidates_binned_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                     (int) binned_smem_bytes<P>());
+	if (e != cudaSuccess) return e;
+	ris_candidates_binned_kernel<P><<<grid, 32 * kBinnedWarps, binned_smem_bytes<P>(), stream>>>(p);
+	return cudaGetLastError();
+}
 
 }  // namespace risltc

@@ -19,7 +19,7 @@ cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cu
 }
 cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid) {
 #if RISLTC_CANDIDATES_BINNED
-	ris_candidates_binned_kernel<ExactNumerics><<<grid, 32 * kBinnedWarps, binned_smem_bytes(), stream>>>(p);
+	return launch_candidates_binned<ExactNumerics>(p, stream, grid);
 #else
 	ris_candidates_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
 #endif

@@ -6,7 +6,7 @@
 namespace risltc {
 cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid) {
 #if RISLTC_CANDIDATES_BINNED
-	ris_candidates_binned_kernel<FastNumerics><<<grid, 32 * kBinnedWarps, binned_smem_bytes(), stream>>>(p);
+	return launch_candidates_binned<FastNumerics>(p, stream, grid);
 #else
 	ris_candidates_kernel<FastNumerics><<<grid, 128, 0, stream>>>(p);
 #endif
