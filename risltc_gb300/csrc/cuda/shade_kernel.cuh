@@ -231,6 +231,23 @@ template <class P> RL_DEV f3 ltc_cp_target(const ShadingData& sd, Ltc ltc, const
 // evaluate_polygonal_light_shading_peters (peters = true,
 // shading_pass.frag.glsl:292-397) and the PSA branch of
 // evaluate_polygonal_light_shading (peters = false, :458-550)
+// One polygon's transform to local space, clip_polygon and
+// prepare_projected_solid_angle_polygon_sampling (shading_pass.frag.glsl:
+// 315-336).  Out of line so that the kernels hold one copy of this long
+// code, shared by the diffuse and specular passes.  Returns the clipped
+// vertex count (0: nothing left, p untouched).
+template <class P>
+__device__ __noinline__ uint32_t prepare_space(mat43 w2l, const Light& l, PsaPolygon& p, bool fa) {
+	const uint32_t n = l.vertex_count;
+	f3 verts[kMaxPolygonVertices];
+#pragma unroll
+	for (int j = 0; j != kMaxLightVertices; ++j)
+		if (j < (int) n) verts[j] = mul_point(w2l, l.v[j]);
+	const uint32_t vc = clip_polygon<P>(n, verts);
+	if (vc != 0) prepare_psa<P>(p, vc, verts, fa);
+	return vc;
+}
+
 // The side flip and both polygons' PSA sampling preparations of
 // evaluate_polygonal_light_shading_peters (shading_pass.frag.glsl:298-341):
 // pd in shading space, ps in cosine space.  Returns false when the estimate
@@ -241,26 +258,8 @@ RL_DEV bool psa_prepare_both(const ShadeParams& pr, const ShadingData& sd, Ltc& 
                              PsaPolygon& ps) {
 	const bool fa = pr.fast_atan != 0;
 	side_flip(ltc, sd, l);
-	uint32_t n = l.vertex_count;
-	// One copy of the clipping and preparation code: both polygons are
-	// prepared into ps, the diffuse one moved to pd before the second pass
-	// (as the reference does to keep its code small).
-#pragma unroll 1
-	for (int i = 0; i != 2; ++i) {
-		if (i > 0) pd = ps;
-		mat43 w2l = (i == 0) ? ltc.world_to_shading : mul(ltc.shading_to_cosine, ltc.world_to_shading);
-		f3 verts[kMaxPolygonVertices];
-#pragma unroll
-		for (int j = 0; j != kMaxLightVertices; ++j)
-			if (j < (int) n) verts[j] = mul_point(w2l, l.v[j]);
-		uint32_t vc = clip_polygon<P>(n, verts);
-		if (vc == 0 && i == 0) return false;
-		if (vc == 0) {
-			ps.psa = 0.0f;
-			break;
-		}
-		prepare_psa<P>(ps, vc, verts, fa);
-	}
+	if (prepare_space<P>(ltc.world_to_shading, l, pd, fa) == 0) return false;
+	if (prepare_space<P>(mul(ltc.shading_to_cosine, ltc.world_to_shading), l, ps, fa) == 0) ps.psa = 0.0f;
 	return pd.psa != 0.0f;
 }
 

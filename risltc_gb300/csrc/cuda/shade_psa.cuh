@@ -109,60 +109,37 @@ RL_DEV void compare_and_swap(PsaPolygon& p, int lhs, int rhs) {
 	p.ellipses[rhs] = swap ? lc : p.ellipses[rhs];
 }
 
-// sort_convex_polygon_vertices, polygon_sampling.glsl:441-506
+// sort_convex_polygon_vertices, polygon_sampling.glsl:441-506: the
+// reference's sorting network for each vertex count (3..8), as a table of
+// compare-and-swap pairs (lhs << 4 | rhs) run in the reference's order, then
+// the three common steps.  One loop instead of a switch keeps the code small.
+// 8-gons clipped to 9 vertices (beyond the reference's networks) use adjacent
+// compare-and-swap passes.
+__device__ __constant__ uint8_t kSortPairs[67] = {
+    0x12,                                                        // 3
+    0x13,                                                        // 4
+    0x24, 0x13, 0x12, 0x03, 0x34,                                // 5
+    0x35, 0x24, 0x15, 0x04, 0x45, 0x13,                          // 6
+    0x25, 0x16, 0x56, 0x34, 0x04, 0x46, 0x13, 0x35, 0x45,        // 7
+    0x26, 0x37, 0x15, 0x04, 0x46, 0x57, 0x67, 0x45, 0x13,        // 8
+    0x01,                                                        // 9: i = 1
+    0x12, 0x01,                                                  //    i = 2
+    0x23, 0x12, 0x01,                                            //    i = 3
+    0x34, 0x23, 0x12, 0x01,                                      //    i = 4
+    0x45, 0x34, 0x23, 0x12, 0x01,                                //    i = 5
+    0x56, 0x45, 0x34, 0x23, 0x12, 0x01,                          //    i = 6
+    0x67, 0x56, 0x45, 0x34, 0x23, 0x12, 0x01,                    //    i = 7
+    0x78, 0x67, 0x56, 0x45, 0x34, 0x23, 0x12, 0x01,              //    i = 8
+};
+// The pairs of vertex count c are kSortPairs[kSortStart[c], kSortStart[c + 1]).
+__device__ __constant__ uint8_t kSortStart[11] = {0, 0, 0, 0, 1, 2, 7, 13, 22, 31, 67};
+
 RL_DEV void sort_convex_polygon_vertices(PsaPolygon& p) {
-	switch (p.vertex_count) {
-	case 3:
-		compare_and_swap(p, 1, 2);
-		break;
-	case 4:
-		compare_and_swap(p, 1, 3);
-		break;
-	case 5:
-		compare_and_swap(p, 2, 4);
-		compare_and_swap(p, 1, 3);
-		compare_and_swap(p, 1, 2);
-		compare_and_swap(p, 0, 3);
-		compare_and_swap(p, 3, 4);
-		break;
-	case 6:
-		compare_and_swap(p, 3, 5);
-		compare_and_swap(p, 2, 4);
-		compare_and_swap(p, 1, 5);
-		compare_and_swap(p, 0, 4);
-		compare_and_swap(p, 4, 5);
-		compare_and_swap(p, 1, 3);
-		break;
-	case 7:
-		compare_and_swap(p, 2, 5);
-		compare_and_swap(p, 1, 6);
-		compare_and_swap(p, 5, 6);
-		compare_and_swap(p, 3, 4);
-		compare_and_swap(p, 0, 4);
-		compare_and_swap(p, 4, 6);
-		compare_and_swap(p, 1, 3);
-		compare_and_swap(p, 3, 5);
-		compare_and_swap(p, 4, 5);
-		break;
-	case 8:
-		compare_and_swap(p, 2, 6);
-		compare_and_swap(p, 3, 7);
-		compare_and_swap(p, 1, 5);
-		compare_and_swap(p, 0, 4);
-		compare_and_swap(p, 4, 6);
-		compare_and_swap(p, 5, 7);
-		compare_and_swap(p, 6, 7);
-		compare_and_swap(p, 4, 5);
-		compare_and_swap(p, 1, 3);
-		break;
-	case 9:
-		// 8-gons clipped to 9 vertices (beyond the reference's networks):
-		// adjacent compare-and-swap passes.
-		for (int i = 1; i != 9; ++i)
-			for (int j = i; j != 0; --j) compare_and_swap(p, j - 1, j);
-		break;
-	default:
-		break;
+	const uint32_t c = p.vertex_count < 10u ? p.vertex_count : 0u;
+	const uint32_t end = kSortStart[c + 1];
+	for (uint32_t k = kSortStart[c]; k < end; ++k) {
+		const uint32_t pair = kSortPairs[k];
+		compare_and_swap(p, (int) (pair >> 4), (int) (pair & 15u));
 	}
 	compare_and_swap(p, 0, 2);
 	if (p.vertex_count >= 4) compare_and_swap(p, 2, 3);
@@ -176,6 +153,7 @@ template <class P> RL_DEV void prepare_psa(PsaPolygon& p, uint32_t vc, const f3 
 	p.vertices[0] = mk2(v[0].x, v[0].y);
 	p.ellipses[0] = ellipse_from_edge<P>(v[0], v[1]);
 	f2 previous = p.ellipses[0];
+#pragma unroll 1
 	for (uint32_t i = 1; i != vc; ++i) {
 		p.vertices[i] = mk2(v[i].x, v[i].y);
 		f2 e = ellipse_from_edge<P>(v[i], v[(i + 1 == vc) ? 0 : i + 1]);
@@ -192,6 +170,7 @@ template <class P> RL_DEV void prepare_psa(PsaPolygon& p, uint32_t vc, const f3 
 	}
 	p.psa = 0.0f;
 	if (is_central_case(p)) {
+#pragma unroll 1
 		for (uint32_t i = 0; i != vc; ++i) {
 			p.sector_psa[i] = ellipse_area_in_sector<P>(p.ellipses[i], p.vertices[i], p.vertices[(i + 1 == vc) ? 0 : i + 1], fa);
 			p.psa += p.sector_psa[i];
@@ -202,6 +181,7 @@ template <class P> RL_DEV void prepare_psa(PsaPolygon& p, uint32_t vc, const f3 
 		float inner_rsd = ellipse_rsqrt_det<P>(inner);
 		f2 outer = mk2(0.0f, 0.0f);
 		float outer_rsd = 0.0f;
+#pragma unroll 1
 		for (uint32_t i = 0; i + 1 != vc; ++i) {
 			f2 ve = p.ellipses[i];
 			bool vi = is_inner_ellipse(ve);
@@ -282,6 +262,7 @@ RL_DEV f2 sample_sector_between_ellipses(f2 rnd, float target_area, f2 inner, f2
 		iterations = (fabsf(rnd.x - 0.5f) <= 0.5f - 1.0e-5f) ? iterations : 0u;
 		float irsd = ellipse_rsqrt_det<P>(inner);
 		float orsd = ellipse_rsqrt_det<P>(outer);
+#pragma unroll 1
 		for (uint32_t i = 0; i != iterations; ++i) {
 			cur = normalize_approx_and_flip(cur, qd1);
 			f2 idir = ellipse_transform(inner, cur);
@@ -308,6 +289,7 @@ template <class P> RL_DEV f3 sample_psa(const PsaPolygon& p, f2 rnd, bool fa, bo
 	f2 xy;
 	if (is_central_case(p)) {
 		f2 outer = mk2(0.0f, 0.0f), d0 = mk2(0.0f, 0.0f);
+#pragma unroll 1
 		for (uint32_t i = 0; i != p.vertex_count; ++i) {
 			if (i > 0) target -= p.sector_psa[i - 1];
 			outer = p.ellipses[i];
@@ -323,6 +305,7 @@ template <class P> RL_DEV f3 sample_psa(const PsaPolygon& p, f2 rnd, bool fa, bo
 	} else {
 		float sector = 0.0f;
 		f2 inner = p.inner_ellipse_0, outer = mk2(0.0f, 0.0f), d0 = mk2(0.0f, 0.0f), d1 = mk2(0.0f, 0.0f);
+#pragma unroll 1
 		for (uint32_t i = 0; i + 1 != p.vertex_count; ++i) {
 			f2 ve = p.ellipses[i];
 			if (i == 0) {
