@@ -299,6 +299,34 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
                           const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
                           uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs);
 
+/* One item of risltc_shade_batch: the arguments of one risltc_shade call. */
+typedef struct risltc_batch_item_s {
+	const risltc_scene_t* scene;
+	risltc_gbuffer_t gbuffer;
+	risltc_settings_t settings;
+	noise_table_t* noise;
+	uint32_t animate, frame_count;
+	float* out_rgb;
+	double* accum;
+	risltc_reservoir_t* reservoirs;
+} risltc_batch_item_t;
+
+/* Streams the items of risltc_shade_batch run on, forked from the context's
+   stream. */
+#define RISLTC_BATCH_STREAMS 8
+
+/* Shades several G-buffers (each with its own scene, settings and noise) in
+ * one call; no counterpart in the reference, which draws one view at a time.
+ * Each item gets its own share of the context's scratch and runs on one of
+ * RISLTC_BATCH_STREAMS streams forked from the context's stream and joined
+ * back to it, so that small frames fill the GPU together.  Results equal the
+ * items' risltc_shade calls bit for bit.  All items are validated before any
+ * work; noise->random_seed of each item advances by its frame_count.  The
+ * first call grows the scratch and creates the streams; later calls with no
+ * larger items allocate nothing, so a batch can be captured into one CUDA
+ * graph. */
+EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* items, uint32_t item_count);
+
 /* Same with host buffers: copies the G-buffer planes in, shades, copies
  * out_rgb back, synchronises and reports device errors.  This is the call a
  * host program makes per frame. */

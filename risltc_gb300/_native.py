@@ -66,6 +66,13 @@ class GBuffer(ctypes.Structure):
                 ("planes", ctypes.c_void_p), ("primitive", ctypes.c_void_p)]
 
 
+class BatchItem(ctypes.Structure):
+    """risltc_batch_item_t."""
+    _fields_ = [("scene", ctypes.c_void_p), ("gbuffer", GBuffer), ("settings", Settings),
+                ("noise", ctypes.POINTER(NoiseTable)), ("animate", ctypes.c_uint32), ("frame_count", ctypes.c_uint32),
+                ("out_rgb", ctypes.c_void_p), ("accum", ctypes.c_void_p), ("reservoirs", ctypes.c_void_p)]
+
+
 class Reservoir(ctypes.Structure):
     _fields_ = [("light_index", ctypes.c_int32), ("w_sum", ctypes.c_float),
                 ("sample_value", ctypes.c_float), ("padding", ctypes.c_uint32)]
@@ -100,6 +107,7 @@ SIGNATURES = {
     "risltc_shade": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer),
                                     ctypes.POINTER(Settings), ctypes.POINTER(NoiseTable), ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "risltc_shade_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_uint32]),
     "risltc_shade_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
                                          c_float_p, c_u32_p, ctypes.POINTER(Settings), ctypes.POINTER(NoiseTable),
                                          ctypes.c_uint32, ctypes.c_uint32, c_float_p]),

@@ -153,6 +153,28 @@ def shade(ctx, scene, gbuffer, width, height, s, noise_seed=0, animate=True, fra
     return nt.random_seed
 
 
+def shade_batch(ctx, items):
+    """risltc_shade_batch.  items: dicts with the keyword arguments of shade()
+    (scene, gbuffer, width, height, settings, noise_seed, animate, frames,
+    out_rgb, accum, reservoirs, primitive).  Returns each item's next noise
+    seed."""
+    lib = _native.load()
+    arr = (_native.BatchItem * len(items))()
+    tables = [_native.NoiseTable(it.get("noise_seed", 0)) for it in items]
+    ptr = (lambda t: None if t is None else t.data_ptr())
+    for a, it, nt in zip(arr, items, tables):
+        a.scene = it["scene"].handle.value
+        prim = it.get("primitive")
+        a.gbuffer = _native.GBuffer(it["width"], it["height"], it["gbuffer"].data_ptr(), ptr(prim))
+        a.settings = it["settings"]
+        a.noise = ctypes.pointer(nt)
+        a.animate = int(it.get("animate", True))
+        a.frame_count = it.get("frames", 1)
+        a.out_rgb, a.accum, a.reservoirs = ptr(it.get("out_rgb")), ptr(it.get("accum")), ptr(it.get("reservoirs"))
+    check(lib.risltc_shade_batch(ctx.handle, arr, len(items)), "risltc_shade_batch")
+    return [nt.random_seed for nt in tables]
+
+
 def shade_host(ctx, scene, gbuffer, width, height, s, noise_seed=0, animate=True, frames=1, primitive=None,
                out=None):
     """risltc_shade_host: numpy in, numpy out (copies and synchronisation inside)."""

@@ -40,6 +40,12 @@ struct risltc_ctx_s {
 	uint32_t* d_light_rays;
 	size_t wavefront_capacity;
 	size_t light_capacity;
+	size_t queue_capacity;  // ray queues (2 words each) in d_ray_count
+	// risltc_shade_batch: items run on these streams, forked from and joined
+	// back to the context's stream.
+	cudaStream_t batch_streams[RISLTC_BATCH_STREAMS];
+	cudaEvent_t batch_fork, batch_join[RISLTC_BATCH_STREAMS];
+	int batch_streams_created;
 	// Kernel timing: five events per shading call (before, between and after
 	// the phases), up to 64 calls between queries.
 	int profiling;
@@ -147,8 +153,16 @@ std::vector<float> child_pair_nodes(const float* nodes, uint32_t node_count) {
 	return out;
 }
 
-int reserve_wavefront(risltc_ctx_t* ctx, size_t pixel_frames, size_t light_count) {
+int reserve_wavefront(risltc_ctx_t* ctx, size_t pixel_frames, size_t light_count, size_t queues = 1) {
 	cudaError_t e = cudaSuccess;
+	if (queues > ctx->queue_capacity) {
+		cudaStreamSynchronize(ctx->stream);
+		cudaFree(ctx->d_ray_count);
+		ctx->d_ray_count = nullptr;
+		ctx->queue_capacity = 0;
+		if ((e = cudaMalloc(&ctx->d_ray_count, 2 * queues * sizeof(uint32_t))) != cudaSuccess) return cuda_status(e);
+		ctx->queue_capacity = queues;
+	}
 	if (light_count > ctx->light_capacity) {
 		cudaStreamSynchronize(ctx->stream);
 		cudaFree(ctx->d_light_rays);
@@ -168,8 +182,7 @@ int reserve_wavefront(risltc_ctx_t* ctx, size_t pixel_frames, size_t light_count
 	ctx->d_rays = nullptr;
 	ctx->d_hits = nullptr;
 	ctx->wavefront_capacity = 0;
-	if (!ctx->d_ray_count) e = cudaMalloc(&ctx->d_ray_count, 2 * sizeof(uint32_t));
-	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_samples, pixel_frames * sizeof(risltc::SampleRecord));
+	e = cudaMalloc(&ctx->d_samples, pixel_frames * sizeof(risltc::SampleRecord));
 	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_staged, 2 * pixel_frames * sizeof(risltc::ShadowRay));
 	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rays, 2 * pixel_frames * sizeof(risltc::ShadowRay));
 	if (e == cudaSuccess) e = cudaMalloc(&ctx->d_hits, 2 * pixel_frames);
@@ -219,6 +232,11 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFree(ctx->d_hits);
 	cudaFree(ctx->d_ray_count);
 	cudaFree(ctx->d_light_rays);
+	for (int i = 0; i < ctx->batch_streams_created; ++i) {
+		cudaStreamDestroy(ctx->batch_streams[i]);
+		cudaEventDestroy(ctx->batch_join[i]);
+	}
+	if (ctx->batch_streams_created) cudaEventDestroy(ctx->batch_fork);
 	for (int i = 0; i < ctx->events_created; ++i)
 		for (int k = 0; k != 5; ++k) cudaEventDestroy(ctx->events[i][k]);
 	free(ctx);
@@ -348,14 +366,55 @@ static int validate_settings(const risltc_settings_t* s) {
 	return RISLTC_OK;
 }
 
-EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
-                          const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
-                          uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs) {
-	if (!ctx || !scene || !gbuffer || !gbuffer->planes || !noise || frame_count == 0 || gbuffer->width == 0 ||
-	    gbuffer->height == 0 || (uint64_t) gbuffer->width * gbuffer->height > 0xffffffffull / 32)
-		return RISLTC_ERROR_INVALID_ARGUMENT;
-	int st = validate_settings(settings);
-	if (st) return st;
+namespace {
+
+bool valid_call(const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer, const noise_table_t* noise,
+                uint32_t frame_count) {
+	return scene && gbuffer && gbuffer->planes && noise && frame_count != 0 && gbuffer->width != 0 &&
+	       gbuffer->height != 0 && (uint64_t) gbuffer->width * gbuffer->height <= 0xffffffffull / 32;
+}
+
+bool uses_ris_pipeline(const risltc_settings_t* s) {
+	return s->polygon_sampling_technique == sample_polygon_ltc_cp && s->light_sampling == light_reservoir &&
+	       s->sample_count_light == 1;
+}
+
+// Shadow rays in their own pass for one sample per technique; the queue's
+// hit slots (2 per pixel-frame) are 32-bit.
+bool uses_ray_queue(const risltc_scene_t* scene, const risltc_settings_t* s, size_t pixel_frames) {
+	return uses_ris_pipeline(s) && s->shadows && scene->view.triangle_count && s->sample_count == 1 &&
+	       pixel_frames < (1ull << 31);
+}
+
+// One call's share of the context's scratch.
+struct Scratch {
+	risltc::ReservoirRecord* records;
+	risltc::SampleRecord* samples;
+	risltc::ShadowRay* staged;
+	risltc::ShadowRay* rays;
+	uint8_t* hits;
+	uint32_t* ray_count;
+	uint32_t* light_rays;
+};
+
+int reserve_records(risltc_ctx_t* ctx, size_t need) {
+	if (need <= ctx->record_capacity) return RISLTC_OK;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_records);
+	ctx->d_records = nullptr;
+	ctx->record_capacity = 0;
+	cudaError_t e = cudaMalloc(&ctx->d_records, need * sizeof(risltc::ReservoirRecord));
+	if (e != cudaSuccess) return cuda_status(e);
+	ctx->record_capacity = need;
+	return RISLTC_OK;
+}
+
+// Enqueues one frame set on `stream` with its scratch already reserved.
+int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const risltc_scene_t* scene,
+              const risltc_gbuffer_t* gbuffer, const risltc_settings_t* settings, uint32_t noise_seed,
+              uint32_t animate, uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs,
+              cudaEvent_t* events) {
 	risltc::ShadeParams p;
 	memset(&p, 0, sizeof(p));
 	p.scene = scene->view;
@@ -372,32 +431,19 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 	p.mis_visibility_estimate = settings->mis_visibility_estimate;
 	p.fast_atan = (int) settings->fast_atan;
 	p.shadows = (int) settings->shadows;
-	p.noise_seed = noise->random_seed;
+	p.noise_seed = noise_seed;
 	p.animate = animate;
 	p.frame_count = frame_count;
 	p.out_rgb = out_rgb;
 	p.accum = accum;
 	p.reservoirs = reservoirs;
 	p.error = ctx->d_error;
-	cudaSetDevice(ctx->device);
 	const size_t pixels = (size_t) gbuffer->width * gbuffer->height;
-	int grid = grid_for(ctx, pixels);
+	const bool fast = settings->numerics == risltc_numerics_fast;
 	cudaError_t e;
-	cudaEvent_t* events = nullptr;
-	if (ctx->profiling && ctx->timed_calls < 64) {
-		int i = ctx->timed_calls++;
-		if (i >= ctx->events_created) {
-			for (int k = 0; k != 5; ++k) cudaEventCreate(&ctx->events[i][k]);
-			ctx->events_created = i + 1;
-		}
-		events = ctx->events[i];
-	}
-	if (settings->polygon_sampling_technique == sample_polygon_ltc_cp && settings->light_sampling == light_reservoir &&
-	    settings->sample_count_light == 1) {
+	if (uses_ris_pipeline(settings)) {
 		// The reference's default configuration: candidate and shading
 		// kernels with reservoir records in between.
-		st = risltc_ctx_reserve(ctx, gbuffer->width, gbuffer->height, frame_count);
-		if (st) return st;
 		risltc::RisParams r;
 		memset(&r, 0, sizeof(r));
 		r.scene = p.scene;
@@ -414,48 +460,136 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		r.noise_seed = p.noise_seed;
 		r.animate = p.animate;
 		r.frame_count = p.frame_count;
-		r.records = ctx->d_records;
-		// Shadow rays in their own pass for one sample per technique; the
-		// queue's hit slots (2 per pixel-frame) are 32-bit.
-		const size_t pixel_frames = pixels * frame_count;
-		if (settings->shadows && scene->view.triangle_count && settings->sample_count == 1 &&
-		    pixel_frames < (1ull << 31)) {
-			st = reserve_wavefront(ctx, pixel_frames, scene->view.light_count);
-			if (st) return st;
-			r.samples = ctx->d_samples;
-			r.staged = ctx->d_staged;
-			r.rays = ctx->d_rays;
-			r.light_rays = ctx->d_light_rays;
-			r.ray_count = ctx->d_ray_count;
-			r.hits = ctx->d_hits;
+		r.records = sc.records;
+		if (uses_ray_queue(scene, settings, pixels * frame_count)) {
+			r.samples = sc.samples;
+			r.staged = sc.staged;
+			r.rays = sc.rays;
+			r.light_rays = sc.light_rays;
+			r.ray_count = sc.ray_count;
+			r.hits = sc.hits;
 		}
 		r.out_rgb = out_rgb;
 		r.accum = accum;
 		r.reservoirs = reservoirs;
 		r.error = ctx->d_error;
-		e = risltc::launch_ris(r, ctx->stream, grid, grid_for(ctx, 2 * pixels * frame_count), events,
-		                       settings->numerics == risltc_numerics_fast);
+		e = risltc::launch_ris(r, stream, grid_for(ctx, pixels), grid_for(ctx, 2 * pixels * frame_count), events,
+		                       fast);
 	} else {
-		e = risltc::launch_shade(p, ctx->stream, grid, events, settings->numerics == risltc_numerics_fast);
+		e = risltc::launch_shade(p, stream, grid_for(ctx, pixels), events, fast);
 	}
-	if (e != cudaSuccess) return cuda_status(e);
+	return e == cudaSuccess ? RISLTC_OK : cuda_status(e);
+}
+
+}  // namespace
+
+EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                          const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
+                          uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs) {
+	if (!ctx || !valid_call(scene, gbuffer, noise, frame_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	int st = validate_settings(settings);
+	if (st) return st;
+	cudaSetDevice(ctx->device);
+	const size_t pixel_frames = (size_t) gbuffer->width * gbuffer->height * frame_count;
+	if (uses_ris_pipeline(settings)) {
+		if ((st = reserve_records(ctx, pixel_frames))) return st;
+		if (uses_ray_queue(scene, settings, pixel_frames) &&
+		    (st = reserve_wavefront(ctx, pixel_frames, scene->view.light_count)))
+			return st;
+	}
+	cudaEvent_t* events = nullptr;
+	if (ctx->profiling && ctx->timed_calls < 64) {
+		int i = ctx->timed_calls++;
+		if (i >= ctx->events_created) {
+			for (int k = 0; k != 5; ++k) cudaEventCreate(&ctx->events[i][k]);
+			ctx->events_created = i + 1;
+		}
+		events = ctx->events[i];
+	}
+	const Scratch sc{ctx->d_records, ctx->d_samples, ctx->d_staged, ctx->d_rays, ctx->d_hits, ctx->d_ray_count,
+	                 ctx->d_light_rays};
+	st = shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise->random_seed, animate, frame_count, out_rgb,
+	               accum, reservoirs, events);
+	if (st) return st;
 	noise->random_seed += frame_count;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* items, uint32_t item_count) {
+	if (!ctx || (!items && item_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (item_count == 0) return RISLTC_OK;
+	// Validate everything before any work; size the scratch for all items.
+	size_t records = 0, wavefront = 0, lights = 0, queues = 0;
+	for (uint32_t i = 0; i != item_count; ++i) {
+		const risltc_batch_item_t& it = items[i];
+		if (!valid_call(it.scene, &it.gbuffer, it.noise, it.frame_count) || it.scene->ctx != ctx)
+			return RISLTC_ERROR_INVALID_ARGUMENT;
+		int st = validate_settings(&it.settings);
+		if (st) return st;
+		const size_t pf = (size_t) it.gbuffer.width * it.gbuffer.height * it.frame_count;
+		if (uses_ris_pipeline(&it.settings)) records += pf;
+		if (uses_ray_queue(it.scene, &it.settings, pf)) {
+			wavefront += pf;
+			lights += (size_t) it.scene->view.light_count;
+			++queues;
+		}
+	}
+	cudaSetDevice(ctx->device);
+	int st;
+	if (records && (st = reserve_records(ctx, records))) return st;
+	if (queues && (st = reserve_wavefront(ctx, wavefront, lights, queues))) return st;
+	cudaError_t e = cudaSuccess;
+	if (!ctx->batch_streams_created) {
+		e = cudaEventCreateWithFlags(&ctx->batch_fork, cudaEventDisableTiming);
+		for (int k = 0; k != RISLTC_BATCH_STREAMS && e == cudaSuccess; ++k) {
+			e = cudaStreamCreateWithFlags(&ctx->batch_streams[k], cudaStreamNonBlocking);
+			if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->batch_join[k], cudaEventDisableTiming);
+			if (e == cudaSuccess) ctx->batch_streams_created = k + 1;
+		}
+		if (e != cudaSuccess) return cuda_status(e);
+	}
+	// Fork: every stream waits for the work already on the context's stream.
+	const int streams = item_count < (uint32_t) RISLTC_BATCH_STREAMS ? (int) item_count : RISLTC_BATCH_STREAMS;
+	if ((e = cudaEventRecord(ctx->batch_fork, ctx->stream)) != cudaSuccess) return cuda_status(e);
+	for (int k = 0; k != streams; ++k)
+		if ((e = cudaStreamWaitEvent(ctx->batch_streams[k], ctx->batch_fork, 0)) != cudaSuccess) return cuda_status(e);
+	size_t r_off = 0, w_off = 0, l_off = 0, q_off = 0;
+	for (uint32_t i = 0; i != item_count; ++i) {
+		const risltc_batch_item_t& it = items[i];
+		const size_t pf = (size_t) it.gbuffer.width * it.gbuffer.height * it.frame_count;
+		Scratch sc{};
+		if (uses_ris_pipeline(&it.settings)) {
+			sc.records = ctx->d_records + r_off;
+			r_off += pf;
+		}
+		if (uses_ray_queue(it.scene, &it.settings, pf)) {
+			sc.samples = ctx->d_samples + w_off;
+			sc.staged = ctx->d_staged + 2 * w_off;
+			sc.rays = ctx->d_rays + 2 * w_off;
+			sc.hits = ctx->d_hits + 2 * w_off;
+			sc.ray_count = ctx->d_ray_count + 2 * q_off;
+			sc.light_rays = ctx->d_light_rays + l_off;
+			w_off += pf;
+			l_off += (size_t) it.scene->view.light_count;
+			++q_off;
+		}
+		st = shade_one(ctx, ctx->batch_streams[i % RISLTC_BATCH_STREAMS], sc, it.scene, &it.gbuffer, &it.settings,
+		               it.noise->random_seed, it.animate, it.frame_count, it.out_rgb, it.accum, it.reservoirs,
+		               nullptr);
+		if (st) return st;
+	}
+	// Join: the context's stream waits for every item.
+	for (int k = 0; k != streams; ++k) {
+		if ((e = cudaEventRecord(ctx->batch_join[k], ctx->batch_streams[k])) != cudaSuccess) return cuda_status(e);
+		if ((e = cudaStreamWaitEvent(ctx->stream, ctx->batch_join[k], 0)) != cudaSuccess) return cuda_status(e);
+	}
+	for (uint32_t i = 0; i != item_count; ++i) items[i].noise->random_seed += items[i].frame_count;
 	return RISLTC_OK;
 }
 
 EXTERN_C int risltc_ctx_reserve(risltc_ctx_t* ctx, uint32_t width, uint32_t height, uint32_t frame_count) {
 	if (!ctx || width == 0 || height == 0 || frame_count == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
-	size_t need = (size_t) width * height * frame_count;
-	if (need <= ctx->record_capacity) return RISLTC_OK;
-	cudaSetDevice(ctx->device);
-	cudaStreamSynchronize(ctx->stream);
-	cudaFree(ctx->d_records);
-	ctx->d_records = nullptr;
-	ctx->record_capacity = 0;
-	cudaError_t e = cudaMalloc(&ctx->d_records, need * sizeof(risltc::ReservoirRecord));
-	if (e != cudaSuccess) return cuda_status(e);
-	ctx->record_capacity = need;
-	return RISLTC_OK;
+	return reserve_records(ctx, (size_t) width * height * frame_count);
 }
 
 static int ensure_staging(risltc_ctx_t* ctx, size_t pixels) {

@@ -21,6 +21,7 @@
 // ris_candidates_kernel and the reservoir sees them in the same order, so the
 // reservoir records are bit-identical.
 #pragma once
+#include <atomic>
 #include "ris_kernels.cuh"
 
 namespace risltc {
@@ -359,12 +360,22 @@ template <class P> constexpr size_t binned_smem_bytes() {
 	return sizeof(WarpTile<BinnedSuper<P>::value>) * kBinnedWarps;
 }
 
-// Launches the binned candidate kernel; its shared memory exceeds the 48 KB
-// available without opting in, so the limit is raised first (per device).
+// Launches the binned candidate kernel.  Its shared memory exceeds the 48 KB
+// available without opting in, so the limit is raised the first time the
+// kernel runs on a device (once, so that later launches, including those
+// captured into a CUDA graph, make no other runtime call).
 template <class P> cudaError_t launch_candidates_binned(const RisParams& p, cudaStream_t stream, int grid) {
-	cudaError_t e = cudaFuncSetAttribute(ris_candidates_binned_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                                     (int) binned_smem_bytes<P>());
+	static std::atomic<uint64_t> configured{0};
+	int device = 0;
+	cudaError_t e = cudaGetDevice(&device);
 	if (e != cudaSuccess) return e;
+	const uint64_t bit = 1ull << (device & 63);
+	if (!(configured.load() & bit)) {
+		e = cudaFuncSetAttribute(ris_candidates_binned_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int) binned_smem_bytes<P>());
+		if (e != cudaSuccess) return e;
+		configured.fetch_or(bit);
+	}
 	ris_candidates_binned_kernel<P><<<grid, 32 * kBinnedWarps, binned_smem_bytes<P>(), stream>>>(p);
 	return cudaGetLastError();
 }

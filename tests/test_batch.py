@@ -1,0 +1,82 @@
+"""Batched shading (risltc_shade_batch): 16 frames of the plane-of-quads form
+(G-buffer on z = 0, quads above it, optional occluders) with mixed
+resolutions, light counts and occluder counts, shaded in one call and in one
+captured CUDA graph, equal bit for bit to one risltc_shade call per frame.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def batch_scenes(count=16, seed=5):
+    import risltc_gb300 as rl
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        # Log-uniform sizes, light counts and occluder counts, scaled down from
+        # the 256^2..1080p, 16..8192-light, 10k..500k-triangle batch workload.
+        w = int(np.exp(rng.uniform(np.log(24), np.log(160))))
+        h = int(np.exp(rng.uniform(np.log(16), np.log(96))))
+        lights = int(np.exp(rng.uniform(np.log(16), np.log(512))))
+        tris = 0 if i % 3 == 0 else int(np.exp(rng.uniform(np.log(500), np.log(5000))))
+        out.append(rl.scenes.plane_of_quads(w, h, lights, seed=seed * 100 + i, triangles=tris))
+    return out
+
+
+def test_batch_and_graph_equal_single_calls(gpu):
+    import torch
+    import risltc_gb300 as rl
+    stream = torch.cuda.Stream()
+    ctx = rl.Context(0, stream=stream.cuda_stream)
+    hss = batch_scenes()
+    scenes = [rl.Scene.from_host_scene(ctx, hs) for hs in hss]
+    s = rl.settings(candidates=8)
+    items, singles = [], []
+    with torch.cuda.stream(stream):
+        for k, (hs, sc) in enumerate(zip(hss, scenes)):
+            g = torch.from_numpy(hs.gbuffer).cuda()
+            frames = 1 + k % 3
+            one = torch.zeros((hs.pixels, 3), dtype=torch.float32, device="cuda")
+            rl.shade(ctx, sc, g, hs.width, hs.height, s, noise_seed=7 * k, frames=frames, out_rgb=one)
+            singles.append(one)
+            items.append(dict(scene=sc, gbuffer=g, width=hs.width, height=hs.height, settings=s, noise_seed=7 * k,
+                              frames=frames, out_rgb=torch.full((hs.pixels, 3), -1.0, device="cuda")))
+        seeds = rl.shade_batch(ctx, items)
+    ctx.check()
+    assert seeds == [7 * k + 1 + k % 3 for k in range(len(items))]
+    for it, one in zip(items, singles):
+        assert torch.equal(it["out_rgb"], one)
+    # The same batch captured into one graph and replayed.
+    for it in items:
+        it["out_rgb"].fill_(-1.0)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        rl.shade_batch(ctx, items)
+    graph.replay()
+    torch.cuda.synchronize()
+    ctx.check()
+    for it, one in zip(items, singles):
+        assert torch.equal(it["out_rgb"], one)
+    for sc in scenes:
+        sc.close()
+    ctx.close()
+
+
+def test_batch_rejects_a_bad_item_before_any_work(gpu):
+    import torch
+    import risltc_gb300 as rl
+    ctx = rl.Context(0)
+    hs = rl.scenes.plane_of_quads(32, 32, 16, seed=1)
+    sc = rl.Scene.from_host_scene(ctx, hs)
+    g = torch.from_numpy(hs.gbuffer).cuda()
+    out = torch.full((hs.pixels, 3), -1.0, device="cuda")
+    good = dict(scene=sc, gbuffer=g, width=hs.width, height=hs.height, settings=rl.settings(), out_rgb=out)
+    bad = dict(good, settings=rl.settings(candidates=0))
+    with pytest.raises(rl.RisltcError):
+        rl.shade_batch(ctx, [good, bad])
+    torch.cuda.synchronize()
+    assert torch.all(out == -1.0)
+    sc.close()
+    ctx.close()
