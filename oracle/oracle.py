@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import build_oracle  # noqa: E402
 
-TECHNIQUE = {"ltc_cp": 4, "projected_solid_angle": 2, "projected_solid_angle_biased": 3}
+TECHNIQUE = {"ltc_cp": 4, "projected_solid_angle": 2, "projected_solid_angle_biased": 3, "area_turk": 1}
 MIS = {"balance": 0, "power": 1, "weighted": 2, "optimal_clamped": 3, "optimal": 4}
 LIGHT_SAMPLING = {"uniform": 0, "ris": 1}
 

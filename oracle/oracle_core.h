@@ -1003,6 +1003,62 @@ static vec3_t psa_mis_shade(const ctx_t* c, const shading_data_t* sd, ltc_coeffi
 	return v3_scale(result, RC(1.0) / (R) st->sample_count);
 }
 
+/* sample_area_polygon_turk, polygon_sampling_related_work.glsl:35-43.  Like
+   the reference, it samples the triangle of vertices 0, 1 and 2 (Turk's
+   square-root parametrisation), not a fan over the whole polygon. */
+static vec3_t sample_area_polygon_turk(const light_t* l, vec2_t random_numbers) {
+	R sqrt_random_0 = R_SQRT(random_numbers.x);
+	R b0 = RC(1.0) - sqrt_random_0, b1 = sqrt_random_0 * random_numbers.y;
+	R b2 = R_FMA(-sqrt_random_0, random_numbers.y, sqrt_random_0);
+	return v3_add(v3_add(v3_scale(l->v[0], b0), v3_scale(l->v[1], b1)), v3_scale(l->v[2], b2));
+}
+
+/* get_polygon_area, shading_pass.frag.glsl:146-150: the area of the triangle
+   of vertices 0, 1 and 2 */
+static R get_polygon_area(const light_t* l) {
+	vec3_t v1 = v3_sub(l->v[1], l->v[0]);
+	vec3_t v2 = v3_sub(l->v[2], l->v[0]);
+	return v3_length(cross_stable(v1, v2)) / RC(2.0);
+}
+
+/* get_area_sample_density, polygon_sampling_related_work.glsl:57-64 */
+static R get_area_sample_density(vec3_t* out_dir, vec3_t light_sample, vec3_t shading_position,
+                                  vec3_t light_normal, R light_area) {
+	vec3_t dir = v3_sub(light_sample, shading_position);
+	R distance_squared = v3_dot(dir, dir);
+	R normalization = RC(1.0) / R_SQRT(distance_squared);
+	dir = v3_scale(dir, normalization);
+	*out_dir = dir;
+	R projected_area = rabs(v3_dot(light_normal, dir)) * light_area;
+	return distance_squared / projected_area;
+}
+
+/* The SAMPLE_POLYGON_AREA_TURK branch of evaluate_polygonal_light_shading
+   (shading_pass.frag.glsl:411-418) with get_polygonal_light_mis_estimate
+   (:281-287) and get_polygon_radiance_brdf_product (:200-207).  With
+   eval_only the stored light_sample is evaluated and no noise is drawn;
+   *visibility is traced only when it comes in true. */
+static vec3_t area_turk_shade(const ctx_t* c, const shading_data_t* sd, const light_t* l, vec3_t* light_sample,
+                              int eval_only, int* visibility, uint32_t* seed) {
+	const oracle_settings_t* st = c->settings;
+	vec3_t result = v3_splat(RC(0.0));
+	vec3_t radiance = V3(l->radiance[0], l->radiance[1], l->radiance[2]);
+	vec3_t light_normal = V3(l->plane[0], l->plane[1], l->plane[2]);
+	for (int i = 0; i != st->sample_count; ++i) {
+		if (!eval_only) *light_sample = sample_area_polygon_turk(l, get_noise_2(seed));
+		vec3_t dir;
+		R density = get_area_sample_density(&dir, *light_sample, sd->position, light_normal, get_polygon_area(l));
+		R lambert = v3_dot(sd->normal, dir);
+		vec3_t rb = v3_splat(RC(0.0));
+		if (v3_dot(sd->normal, dir) > RC(0.0)) {
+			*visibility = get_polygon_visibility(c->scene, *visibility, dir, sd->position, l);
+			rb = v3_mul(radiance, evaluate_brdf(sd, dir));
+		}
+		result = v3_add(result, (density > RC(0.0)) ? v3_scale(rb, lambert / density) : v3_splat(RC(0.0)));
+	}
+	return v3_scale(result, RC(1.0) / (R) st->sample_count);
+}
+
 /* Per-pixel body of the shading pass, shading_pass.frag.glsl:674-770 */
 static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed, R out_rgb[3],
                         oracle_reservoir_t* out_res) {
@@ -1014,6 +1070,10 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 	ltc_coefficients_t ltc =
 	    get_ltc_coefficients(s, fresnel_luminance, sd->roughness, sd->position, sd->normal, sd->outgoing);
 	int peters = st->polygon_sampling_technique == ORACLE_TECHNIQUE_LTC_CP;
+	int area_turk = st->polygon_sampling_technique == ORACLE_TECHNIQUE_AREA_TURK;
+	/* The sampled light position of the area technique, carried from
+	   candidate to candidate and stored in the reservoir (:704, 735). */
+	vec3_t light_sample = v3_splat(RC(0.0));
 	if (out_res) {
 		out_res->light_index = -1;
 		out_res->w_sum = 0.0;
@@ -1025,16 +1085,20 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 			if (light_idx > n - 1) light_idx = n - 1;
 			light_t l;
 			load_light(s, light_idx, &l);
-			vec3_t result = v3_scale(psa_mis_shade(c, sd, ltc, &l, &seed, peters, 1), (R) n);
+			int visibility = 1;
+			vec3_t shade = area_turk ? area_turk_shade(c, sd, &l, &light_sample, 0, &visibility, &seed)
+			                         : psa_mis_shade(c, sd, ltc, &l, &seed, peters, 1);
+			vec3_t result = v3_scale(shade, (R) n);
 			R ls = (R) st->light_samples;
 			result = V3(result.x / ls, result.y / ls, result.z / ls);
-			final_color = v3_add(final_color, v3_scale(result, RC(1.0)));
+			final_color = v3_add(final_color, v3_scale(result, visibility ? RC(1.0) : RC(0.0)));
 			if (out_res && i == 0) out_res->light_index = light_idx;
 		}
 	} else {
 		for (int j = 0; j != st->light_samples; ++j) {
 			R w_sum = RC(0.0), sample_value = RC(0.0);
 			int res_index = -1;
+			vec3_t res_light_sample = v3_splat(RC(0.0));
 			int m = st->candidate_count;
 			for (int i = 0; i != m; ++i) {
 				int light_idx = (int) (get_noise_1(&seed) * (R) n);
@@ -1042,10 +1106,14 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 				light_t l;
 				load_light(s, light_idx, &l);
 				vec3_t color;
-				if (peters)
+				if (peters) {
 					color = ltc_cp_target(c, sd, ltc, &l);
-				else
+				} else if (area_turk) {
+					int dummy_visibility = 0;
+					color = area_turk_shade(c, sd, &l, &light_sample, 0, &dummy_visibility, &seed);
+				} else {
 					color = psa_mis_shade(c, sd, ltc, &l, &seed, 0, 0);
+				}
 				R p_hat = v3_length(color);
 				R p = RC(1.0) / (R) n;
 				R w = p_hat / p;
@@ -1054,6 +1122,7 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 				w_sum += w;
 				if (w > RC(0.0) && rnd < (w / w_sum)) {
 					res_index = light_idx;
+					res_light_sample = light_sample;
 					sample_value = p_hat;
 				}
 			}
@@ -1065,10 +1134,15 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 			if (res_index >= 0) {
 				light_t l;
 				load_light(s, res_index, &l);
-				vec3_t color = psa_mis_shade(c, sd, ltc, &l, &seed, peters, 1);
+				int visibility = 1;
+				vec3_t color = area_turk ? area_turk_shade(c, sd, &l, &res_light_sample, 1, &visibility, &seed)
+				                         : psa_mis_shade(c, sd, ltc, &l, &seed, peters, 1);
 				R p_hat = sample_value;
 				R W = w_sum / ((R) m * p_hat);
-				if (p_hat == RC(0.0)) W = RC(0.0);
+				/* The area technique has no p_hat == 0 guard but multiplies
+				   by the traced visibility (:749-756). */
+				if (!area_turk && p_hat == RC(0.0)) W = RC(0.0);
+				if (area_turk) W = W * (visibility ? RC(1.0) : RC(0.0));
 				vec3_t cw = v3_scale(color, W);
 				R ls = (R) st->light_samples;
 				final_color = v3_add(final_color, V3(cw.x / ls, cw.y / ls, cw.z / ls));

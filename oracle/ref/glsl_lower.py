@@ -8,10 +8,11 @@ and its includes).  To run *that code itself* on the CPU, this module reads the
 files where they lie, applies purely mechanical rewrites, and returns C++ text
 that is piped straight into g++ (nothing is written to disk):
 
-  * #include "x.glsl" is inlined (once per file); the related-work sampler
-    library (polygon_sampling_related_work.glsl, only used by the
-    SAMPLE_POLYGON_AREA_TURK branch, which is compiled out) is replaced by the
-    polygon_sampling.glsl it includes;
+  * #include "x.glsl" is inlined (once per file); of the related-work
+    sampler library (polygon_sampling_related_work.glsl) only the two
+    functions of the SAMPLE_POLYGON_AREA_TURK branch (sample_area_polygon_turk
+    and get_area_sample_density) are kept, after the polygon_sampling.glsl it
+    includes (its solid-angle samplers and cubic solver are not on the path);
   * comments, #version and #extension lines are dropped;
   * parameter qualifiers: `inout T x` / `out T x` become `T& x`, `in T x`
     becomes `T x`, array parameters keep their (pointer) form;
@@ -32,11 +33,32 @@ import re
 INCLUDE_RE = re.compile(r'^\s*#include\s+"([^"]+)"\s*$', re.M)
 
 
+AREA_TURK_FUNCTIONS = ("vec3 sample_area_polygon_turk(", "float get_area_sample_density(")
+
+
+def _function_text(text, signature_start):
+    """The full definition of the function whose signature starts with
+    signature_start (up to its matching closing brace)."""
+    i = text.index(signature_start)
+    j = text.index("{", i)
+    depth = 0
+    for k in range(j, len(text)):
+        depth += {"{": 1, "}": -1}.get(text[k], 0)
+        if depth == 0:
+            return text[i:k + 1] + "\n"
+    raise ValueError("unbalanced braces after " + signature_start)
+
+
 def _inline(path, shader_dir, seen):
     name = os.path.basename(path)
     if name == "polygon_sampling_related_work.glsl":
-        name = "polygon_sampling.glsl"
-        path = os.path.join(shader_dir, name)
+        if name in seen:
+            return ""
+        seen.add(name)
+        with open(path, "r") as f:
+            related = _strip_comments(f.read())
+        base = _inline(os.path.join(shader_dir, "polygon_sampling.glsl"), shader_dir, seen)
+        return base + "\n" + "".join(_function_text(related, sig) for sig in AREA_TURK_FUNCTIONS)
     if name in seen:
         return ""
     seen.add(name)

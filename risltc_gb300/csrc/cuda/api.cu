@@ -355,7 +355,8 @@ static int validate_settings(const risltc_settings_t* s) {
 	if (!s) return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (s->polygon_sampling_technique != sample_polygon_ltc_cp &&
 	    s->polygon_sampling_technique != sample_polygon_projected_solid_angle &&
-	    s->polygon_sampling_technique != sample_polygon_projected_solid_angle_biased)
+	    s->polygon_sampling_technique != sample_polygon_projected_solid_angle_biased &&
+	    s->polygon_sampling_technique != sample_polygon_area_turk)
 		return RISLTC_ERROR_UNSUPPORTED;
 	if ((int) s->mis_heuristic < 0 || s->mis_heuristic >= mis_heuristic_count) return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (s->light_sampling != light_uniform && s->light_sampling != light_reservoir) return RISLTC_ERROR_INVALID_ARGUMENT;

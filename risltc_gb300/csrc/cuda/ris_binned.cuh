@@ -41,8 +41,11 @@ constexpr int kDeferred = kItems + 32;       // deferred items pending at most
 
 // Candidates per pixel per super-chunk (measured best: 32 in exact numerics,
 // 16 in fast numerics, where the smaller tile leaves more L1 for the lights).
+#ifndef RISLTC_BINNED_SUPER_EXACT
+#define RISLTC_BINNED_SUPER_EXACT 32
+#endif
 template <class P> struct BinnedSuper {
-	static constexpr int value = 32;
+	static constexpr int value = RISLTC_BINNED_SUPER_EXACT;
 };
 template <> struct BinnedSuper<FastNumerics> {
 	static constexpr int value = 16;

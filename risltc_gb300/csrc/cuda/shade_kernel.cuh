@@ -332,11 +332,58 @@ RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, c
 
 // Body of shading_pass.frag.glsl:main (:674-770) for one pixel and frame.
 // C is the numerics of the RIS candidate evaluation, P of everything else.
+// sample_area_polygon_turk, polygon_sampling_related_work.glsl:35-43.  Like
+// the reference, it samples the triangle of vertices 0, 1 and 2.
+RL_DEV f3 sample_area_polygon_turk(const Light& l, f2 rnd) {
+	const float s = __fsqrt_rn(rnd.x);
+	const float b0 = 1.0f - s, b1 = s * rnd.y, b2 = __fmaf_rn(-s, rnd.y, s);
+	return add(add(scale(l.v[0], b0), scale(l.v[1], b1)), scale(l.v[2], b2));
+}
+
+// get_polygon_area, shading_pass.frag.glsl:146-150 (vertices 0, 1, 2)
+template <class P> RL_DEV float polygon_area(const Light& l) {
+	const f3 c = cross_stable(sub(l.v[1], l.v[0]), sub(l.v[2], l.v[0]));
+	return P::div(P::sqrt(dot(c, c)), 2.0f);
+}
+
+// The SAMPLE_POLYGON_AREA_TURK branch of evaluate_polygonal_light_shading
+// (shading_pass.frag.glsl:411-418) with get_area_sample_density
+// (polygon_sampling_related_work.glsl:57-64), get_polygonal_light_mis_estimate
+// (:281-287) and get_polygon_radiance_brdf_product (:200-207).  With
+// eval_only the stored light_sample is evaluated and no noise is drawn;
+// visibility is traced only when it comes in true.
+template <class P>
+RL_DEV f3 area_turk_shade(const ShadeParams& pr, const ShadingData& sd, const Light& l, f3& light_sample,
+                          bool eval_only, bool& visibility, uint32_t& seed) {
+	f3 result = splat(0.0f);
+	const f3 normal = mk3(l.plane[0], l.plane[1], l.plane[2]);
+	for (int i = 0; i != pr.sample_count; ++i) {
+		if (!eval_only) light_sample = sample_area_polygon_turk(l, get_noise_2(seed));
+		f3 dir = sub(light_sample, sd.position);
+		const float d2 = dot(dir, dir);
+		dir = scale(dir, P::rsqrt(d2));
+		const float projected_area = fabsf(dot(normal, dir)) * polygon_area<P>(l);
+		const float density = P::div(d2, projected_area);
+		const float lambert = dot(sd.normal, dir);
+		f3 rb = splat(0.0f);
+		if (dot(sd.normal, dir) > 0.0f) {
+			visibility = polygon_visibility<P>(pr, visibility, dir, sd.position, l);
+			rb = mul(l.radiance, evaluate_brdf<P>(sd, dir));
+		}
+		result = add(result, density > 0.0f ? scale(rb, P::div(lambert, density)) : splat(0.0f));
+	}
+	return scale(result, P::rcp((float) pr.sample_count));
+}
+
 template <class C, class P>
 RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& ltc, uint32_t seed, bool first_frame,
                       risltc_reservoir_t* res_out) {
 	const int n = pr.scene.light_count;
 	const bool peters = pr.technique == sample_polygon_ltc_cp;
+	const bool area_turk = pr.technique == sample_polygon_area_turk;
+	// The area technique's sampled light position, carried from candidate to
+	// candidate and kept by the reservoir (shading_pass.frag.glsl:704, 735).
+	f3 light_sample = splat(0.0f);
 	f3 final_color = splat(0.0f);
 	risltc_reservoir_t rec;
 	rec.light_index = -1;
@@ -349,16 +396,20 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 			idx = idx > n - 1 ? n - 1 : idx;
 			Light l;
 			load_light(pr.scene, idx, l);
-			f3 r = scale(psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true), (float) n);
+			bool visibility = true;
+			const f3 shade = area_turk ? area_turk_shade<P>(pr, sd, l, light_sample, false, visibility, seed)
+			                           : psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true);
+			f3 r = scale(shade, (float) n);
 			float ls = (float) pr.light_samples;
 			r = mk3(P::div(r.x, ls), P::div(r.y, ls), P::div(r.z, ls));
-			final_color = add(final_color, scale(r, 1.0f));
+			final_color = add(final_color, scale(r, visibility ? 1.0f : 0.0f));
 			if (i == 0) rec.light_index = idx;
 		}
 	} else {
 		for (int j = 0; j != pr.light_samples; ++j) {
 			float w_sum = 0.0f, sample_value = 0.0f;
 			int res_index = -1;
+			f3 res_light_sample = splat(0.0f);
 			const int m = pr.candidate_count;
 			const float p = P::rcp((float) n);
 			for (int i = 0; i != m; ++i) {
@@ -366,7 +417,15 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 				idx = idx > n - 1 ? n - 1 : idx;
 				Light l;
 				load_light(pr.scene, idx, l);
-				f3 color = peters ? ltc_cp_target<C>(sd, ltc, l) : psa_mis_shade<C>(pr, sd, ltc, l, seed, false, false);
+				f3 color;
+				if (peters) {
+					color = ltc_cp_target<C>(sd, ltc, l);
+				} else if (area_turk) {
+					bool dummy_visibility = false;
+					color = area_turk_shade<C>(pr, sd, l, light_sample, false, dummy_visibility, seed);
+				} else {
+					color = psa_mis_shade<C>(pr, sd, ltc, l, seed, false, false);
+				}
 				float p_hat = C::sqrt(dot(color, color));
 				float w = C::div(p_hat, p);
 				// insert_in_reservoir, reservoir.glsl:34-41
@@ -374,6 +433,7 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 				w_sum += w;
 				if (w > 0.0f && rnd < C::div(w, w_sum)) {
 					res_index = idx;
+					res_light_sample = light_sample;
 					sample_value = p_hat;
 				}
 			}
@@ -385,9 +445,14 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 			if (res_index >= 0) {
 				Light l;
 				load_light(pr.scene, res_index, l);
-				f3 color = psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true);
+				bool visibility = true;
+				const f3 color = area_turk ? area_turk_shade<P>(pr, sd, l, res_light_sample, true, visibility, seed)
+				                           : psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true);
 				float W = P::div(w_sum, (float) m * sample_value);
-				if (sample_value == 0.0f) W = 0.0f;
+				// The area technique has no p_hat == 0 guard but multiplies by
+				// the traced visibility (shading_pass.frag.glsl:749-756).
+				if (!area_turk && sample_value == 0.0f) W = 0.0f;
+				if (area_turk) W = W * (visibility ? 1.0f : 0.0f);
 				f3 cw = scale(color, W);
 				float ls = (float) pr.light_samples;
 				final_color = add(final_color, mk3(P::div(cw.x, ls), P::div(cw.y, ls), P::div(cw.z, ls)));

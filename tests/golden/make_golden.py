@@ -59,6 +59,8 @@ CONFIGS = {
     "hf_psa_biased": ("hf", {"light_sampling": "uniform", "technique": "projected_solid_angle_biased"}, 0),
     "tris_m8": ("tris", {"m": 8}, 2),
     "octagons_m8": ("oct", {"m": 8}, 0),
+    "hf_area_turk_m8": ("hf", {"m": 8, "technique": "area_turk"}, 0),
+    "hf_uniform_area_turk": ("hf", {"light_sampling": "uniform", "technique": "area_turk"}, 1),
 }
 
 

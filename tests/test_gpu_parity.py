@@ -97,7 +97,8 @@ def test_exact_kernel_matches_oracle_bit_exact(rl, name):
         assert np.array_equal(wp[:, 1], ores["sample_value"].astype(np.float32))
 
 
-@pytest.mark.parametrize("name", ["quads_m8", "quads_m32", "tris_m8", "hf_psa_ris_m8", "hf_uniform_psa"])
+@pytest.mark.parametrize("name", ["quads_m8", "quads_m32", "tris_m8", "hf_psa_ris_m8", "hf_uniform_psa",
+                                  "hf_area_turk_m8", "hf_uniform_area_turk"])
 def test_exact_kernel_matches_reference_fixture(rl, name):
     c = gd.config(name)
     sc = gd.scene(c["scene"])
@@ -204,5 +205,5 @@ def test_background_pixels_and_argument_errors(rl):
     with pytest.raises(rlm.RisltcError):
         rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(candidates=0), out_rgb=out)
     with pytest.raises(rlm.RisltcError):
-        rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(technique="area_turk"), out_rgb=out)
+        rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(technique="baseline"), out_rgb=out)
     scene.close()
