@@ -211,6 +211,30 @@ typedef struct risltc_bvh_s {
 EXTERN_C int risltc_bvh_build(risltc_bvh_t* bvh, const float* triangles, uint32_t triangle_count, uint32_t max_leaf_size);
 EXTERN_C void risltc_bvh_destroy(risltc_bvh_t* bvh);
 
+/* first_person_camera_t, src/camera.h:29-49 (48 bytes), as stored at the
+   start of a quicksave file. */
+typedef struct risltc_camera_s {
+	float position_world_space[3];
+	float rotation_z, rotation_x, vertical_fov;
+	float near_plane, far_plane, speed;
+	int32_t rotate_camera;
+	float rotation_x_0, rotation_z_0;
+} risltc_camera_t;
+
+/* quick_load, src/main.c:76-125: reads a quicksave file (camera, then lights
+   with their plane-space vertices and texture paths; legacy files with
+   scaling_y <= 0 get scaling_y = scaling_x) and returns the lights with their
+   derived members updated (update_polygonal_light).  camera may be NULL.
+   Free the lights with risltc_destroy_lights.  RISLTC_ERROR_IO on a missing,
+   short or implausible file. */
+EXTERN_C int risltc_quick_load(const char* path, risltc_camera_t* camera, polygonal_light_t** lights,
+                               uint32_t* light_count);
+/* quick_save, src/main.c:45-71: writes the same format. */
+EXTERN_C int risltc_quick_save(const char* path, const risltc_camera_t* camera, const polygonal_light_t* lights,
+                               uint32_t light_count);
+/* destroy_polygonal_light on each light, then frees the array. */
+EXTERN_C void risltc_destroy_lights(polygonal_light_t* lights, uint32_t light_count);
+
 /* Run settings: render_settings_t (src/main.h:123-156) reduced to what the
    shading pass reads, plus the candidate count the reference hard-codes
    (shading_pass.frag.glsl:726, 32). */

@@ -66,6 +66,14 @@ class GBuffer(ctypes.Structure):
                 ("planes", ctypes.c_void_p), ("primitive", ctypes.c_void_p)]
 
 
+class Camera(ctypes.Structure):
+    """risltc_camera_t = first_person_camera_t, src/camera.h:29-49."""
+    _fields_ = [("position_world_space", ctypes.c_float * 3), ("rotation_z", ctypes.c_float),
+                ("rotation_x", ctypes.c_float), ("vertical_fov", ctypes.c_float), ("near_plane", ctypes.c_float),
+                ("far_plane", ctypes.c_float), ("speed", ctypes.c_float), ("rotate_camera", ctypes.c_int32),
+                ("rotation_x_0", ctypes.c_float), ("rotation_z_0", ctypes.c_float)]
+
+
 class BatchItem(ctypes.Structure):
     """risltc_batch_item_t."""
     _fields_ = [("scene", ctypes.c_void_p), ("gbuffer", GBuffer), ("settings", Settings),
@@ -96,6 +104,11 @@ SIGNATURES = {
     "risltc_ltc_table_destroy": (None, [ctypes.POINTER(LtcTable)]),
     "risltc_bvh_build": (ctypes.c_int, [ctypes.POINTER(Bvh), c_float_p, ctypes.c_uint32, ctypes.c_uint32]),
     "risltc_bvh_destroy": (None, [ctypes.POINTER(Bvh)]),
+    "risltc_quick_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Camera),
+                                         ctypes.POINTER(ctypes.POINTER(PolygonalLight)), c_u32_p]),
+    "risltc_quick_save": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Camera), ctypes.POINTER(PolygonalLight),
+                                         ctypes.c_uint32]),
+    "risltc_destroy_lights": (None, [ctypes.POINTER(PolygonalLight), ctypes.c_uint32]),
     "risltc_default_settings": (None, [ctypes.POINTER(Settings)]),
     "risltc_ctx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]),
     "risltc_ctx_destroy": (None, [ctypes.c_void_p]),

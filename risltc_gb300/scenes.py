@@ -18,6 +18,7 @@ std140 packing of write_lights); any library exporting
 set_polygonal_light_vertex_count and update_polygonal_light can be passed in.
 """
 import ctypes
+import os
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -98,6 +99,41 @@ def build_lights(specs, lib=None):
             row[12 + 4 * v:15 + 4 * v] = world[v if v < n else 0, :3]
         lib.destroy_polygonal_light(ctypes.byref(light)) if hasattr(lib, "destroy_polygonal_light") else None
     return out, maxv
+
+
+def load_quicksave(path):
+    """risltc_quick_load: the camera (risltc_camera_t), the lights' std140
+    buffer (write_lights layout) and the maximum vertex count of a quicksave
+    file (src/main.c:76-125)."""
+    lib = _native.load()
+    camera = _native.Camera()
+    lights = ctypes.POINTER(_native.PolygonalLight)()
+    count = ctypes.c_uint32(0)
+    _native.check(lib.risltc_quick_load(os.fsencode(path), ctypes.byref(camera), ctypes.byref(lights),
+                                        ctypes.byref(count)), "risltc_quick_load")
+    try:
+        maxv = max(3, int(lib.risltc_max_light_vertex_count(lights, count.value)))
+        buf = np.zeros((count.value, 12 + 4 * maxv), np.float32)
+        _native.check(lib.risltc_write_lights(buf.ctypes.data_as(_native.c_float_p), lights, count.value, maxv),
+                      "risltc_write_lights")
+    finally:
+        lib.risltc_destroy_lights(lights, count.value)
+    return camera, buf, maxv
+
+
+def resave_quicksave(src, dst):
+    """Loads a quicksave file and writes it again with risltc_quick_save."""
+    lib = _native.load()
+    camera = _native.Camera()
+    lights = ctypes.POINTER(_native.PolygonalLight)()
+    count = ctypes.c_uint32(0)
+    _native.check(lib.risltc_quick_load(os.fsencode(src), ctypes.byref(camera), ctypes.byref(lights),
+                                        ctypes.byref(count)), "risltc_quick_load")
+    try:
+        _native.check(lib.risltc_quick_save(os.fsencode(dst), ctypes.byref(camera), lights, count.value),
+                      "risltc_quick_save")
+    finally:
+        lib.risltc_destroy_lights(lights, count.value)
 
 
 def synthetic_ltc(seed=0, size=64):
