@@ -235,6 +235,16 @@ EXTERN_C int risltc_quick_save(const char* path, const risltc_camera_t* camera, 
 /* destroy_polygonal_light on each light, then frees the array. */
 EXTERN_C void risltc_destroy_lights(polygonal_light_t* lights, uint32_t light_count);
 
+/* Light clusters (no counterpart in the reference, which draws RIS
+   candidates uniformly over all lights): k-means with k-means++ seeding of
+   the lights' centres (centers: light_count x 3 floats) into cluster_count
+   clusters, deterministic for a seed (double arithmetic, splitmix64).
+   order (light_count entries) lists the lights cluster by cluster, ascending
+   inside a cluster; cluster c holds order[offsets[c] .. offsets[c + 1])
+   (offsets: cluster_count + 1 entries; a cluster may be empty). */
+EXTERN_C int risltc_cluster_lights(const float* centers, uint32_t light_count, uint32_t cluster_count,
+                                   uint64_t seed, uint32_t iterations, uint32_t* order, uint32_t* offsets);
+
 /* Run settings: render_settings_t (src/main.h:123-156) reduced to what the
    shading pass reads, plus the candidate count the reference hard-codes
    (shading_pass.frag.glsl:726, 32). */

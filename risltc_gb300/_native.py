@@ -109,6 +109,8 @@ SIGNATURES = {
     "risltc_quick_save": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Camera), ctypes.POINTER(PolygonalLight),
                                          ctypes.c_uint32]),
     "risltc_destroy_lights": (None, [ctypes.POINTER(PolygonalLight), ctypes.c_uint32]),
+    "risltc_cluster_lights": (ctypes.c_int, [c_float_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                             ctypes.c_uint32, c_u32_p, c_u32_p]),
     "risltc_default_settings": (None, [ctypes.POINTER(Settings)]),
     "risltc_ctx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]),
     "risltc_ctx_destroy": (None, [ctypes.c_void_p]),

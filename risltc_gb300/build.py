@@ -16,7 +16,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librisltc_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-HOST_SOURCES = ["host/light.c", "host/ltc_table.c", "host/bvh.c", "host/quicksave.c"]
+HOST_SOURCES = ["host/light.c", "host/ltc_table.c", "host/bvh.c", "host/quicksave.c", "host/clusters.c"]
 CUDA_SOURCES = {
     "cuda/shade_exact.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "cuda/shade_fast.cu": ["--fmad=true", "-prec-div=true", "-prec-sqrt=true"],

@@ -136,6 +136,33 @@ def resave_quicksave(src, dst):
         lib.risltc_destroy_lights(lights, count.value)
 
 
+def light_centers(lights_std140):
+    """Mean of each light's world-space vertices (std140 rows)."""
+    n = lights_std140[:, 8].view(np.uint32).astype(np.int64)
+    maxv = (lights_std140.shape[1] - 12) // 4
+    verts = lights_std140[:, 12:12 + 4 * maxv].reshape(-1, maxv, 4)[:, :, :3].astype(np.float64)
+    mask = np.arange(maxv)[None, :] < n[:, None]
+    return ((verts * mask[:, :, None]).sum(1) / n[:, None]).astype(np.float32)
+
+
+def cluster_lights(hs, cluster_count, seed=0, iterations=32):
+    """risltc_cluster_lights on the scene's light centres.  Returns a copy of
+    the scene with its lights (and light specs) listed cluster by cluster, and
+    the cluster offsets (cluster c holds lights offsets[c] .. offsets[c + 1])."""
+    lib = _native.load()
+    centers = np.ascontiguousarray(light_centers(hs.lights))
+    n = centers.shape[0]
+    order = np.zeros(n, np.uint32)
+    offsets = np.zeros(cluster_count + 1, np.uint32)
+    _native.check(lib.risltc_cluster_lights(centers.ctypes.data_as(_native.c_float_p), n, cluster_count, seed,
+                                            iterations, order.ctypes.data_as(_native.c_u32_p),
+                                            offsets.ctypes.data_as(_native.c_u32_p)), "risltc_cluster_lights")
+    specs = [hs.light_specs[i] for i in order] if hs.light_specs else []
+    out = HostScene(hs.width, hs.height, hs.gbuffer, hs.primitive, np.ascontiguousarray(hs.lights[order]),
+                    hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants, hs.triangles, specs)
+    return out, offsets
+
+
 def synthetic_ltc(seed=0, size=64):
     """The product's seeded synthetic LTC table (risltc_ltc_table_synthetic)."""
     lib = _native.load()
