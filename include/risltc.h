@@ -245,6 +245,15 @@ EXTERN_C void risltc_destroy_lights(polygonal_light_t* lights, uint32_t light_co
 EXTERN_C int risltc_cluster_lights(const float* centers, uint32_t light_count, uint32_t cluster_count,
                                    uint64_t seed, uint32_t iterations, uint32_t* order, uint32_t* offsets);
 
+/* Summaries of clusters (offsets as for risltc_cluster_lights, lights as the
+   std140 rows of risltc_write_lights listed cluster by cluster): per cluster
+   a bounding sphere (bounds: centre xyz = mean of the lights' vertices,
+   radius rounded up) and the power (power: sum over its lights of the
+   radiance's luminance times the polygon's area).  Used by
+   risltc_scene_set_clusters. */
+EXTERN_C int risltc_cluster_summaries(const float* lights_std140, uint32_t light_count, uint32_t max_vertex_count,
+                                      const uint32_t* offsets, uint32_t cluster_count, float* bounds, float* power);
+
 /* Run settings: render_settings_t (src/main.h:123-156) reduced to what the
    shading pass reads, plus the candidate count the reference hard-codes
    (shading_pass.frag.glsl:726, 32). */
@@ -260,6 +269,12 @@ typedef enum risltc_numerics_e {
 	risltc_numerics_fast = 1
 } risltc_numerics_t;
 
+typedef enum risltc_proposal_e {
+	risltc_proposal_uniform = 0,  /* p = 1 / N (shading_pass.frag.glsl:733) */
+	risltc_proposal_clusters = 1, /* cluster weights: power over distance with a cosine bound */
+	risltc_proposal_learned = 2   /* cluster weights: softmax of a learned model's logits */
+} risltc_proposal_t;
+
 typedef struct risltc_settings_s {
 	sample_polygon_technique_t polygon_sampling_technique; /* ltc_cp or projected_solid_angle(_biased) */
 	light_sampling_strategies_t light_sampling;
@@ -271,6 +286,11 @@ typedef struct risltc_settings_s {
 	uint32_t fast_atan;
 	uint32_t shadows;           /* trace shadow rays through the scene BVH */
 	risltc_numerics_t numerics;
+	/* Source of the RIS candidates (default configuration only): uniform
+	   over all lights as in the reference, or the cluster proposal of
+	   risltc_scene_set_clusters mixed with uniform sampling. */
+	risltc_proposal_t proposal;
+	float proposal_uniform_fraction; /* in (0, 1]: weight of the uniform part */
 } risltc_settings_t;
 
 /* specify_default_render_settings, src/main.c:220-236 (M = 32, shadows on) */
@@ -301,6 +321,14 @@ typedef struct risltc_scene_s risltc_scene_t;
 /* stream: a cudaStream_t, or NULL for the legacy default stream. */
 EXTERN_C int risltc_ctx_create(risltc_ctx_t** ctx, int device, void* stream);
 EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx);
+
+/* Gives the scene's lights a cluster structure for the cluster proposal:
+   cluster c holds lights offsets[c] .. offsets[c + 1] (the lights must be
+   listed cluster by cluster, e.g. in the order of risltc_cluster_lights;
+   offsets[0] = 0, offsets[cluster_count] = light_count, at most 1024
+   clusters).  Derives each cluster's bounding sphere and power (luminance x
+   area summed over its lights) and uploads them. */
+EXTERN_C int risltc_scene_set_clusters(risltc_scene_t* scene, const uint32_t* offsets, uint32_t cluster_count);
 
 /* Uploads lights (the std140 buffer of risltc_write_lights), the LTC table
    and, if triangle_count > 0, builds and uploads the BVH of the occluders

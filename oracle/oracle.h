@@ -47,6 +47,14 @@ typedef struct oracle_scene_s {
 	int32_t triangle_count;
 	const float* bvh_nodes; /* NULL: brute-force shadow queries */
 	int32_t bvh_node_count;
+	/* Light clusters for the cluster proposal (lights listed cluster by
+	   cluster): offsets (count + 1), each light's cluster, each cluster's
+	   bounding sphere (centre xyz, radius) and power. */
+	const uint32_t* cluster_offsets;
+	const uint32_t* light_cluster;
+	const float* cluster_bounds;
+	const float* cluster_power;
+	int32_t cluster_count;
 } oracle_scene_t;
 
 typedef struct oracle_settings_s {
@@ -61,6 +69,11 @@ typedef struct oracle_settings_s {
 	/* 1: reproduce the reference's calculate_ltc over all array slots and its
 	   8-vertex clip aliasing (for pinning against the reference itself). */
 	int32_t reference_slots;
+	/* 1: RIS candidates from the cluster proposal (risltc_proposal_clusters)
+	   with the given uniform fraction and the frame's second noise number. */
+	int32_t proposal;
+	float proposal_uniform_fraction;
+	uint32_t random_number_proposal;
 } oracle_settings_t;
 
 typedef struct oracle_gbuffer_s {

@@ -23,7 +23,10 @@ class Scene(ctypes.Structure):
                 ("max_light_vertex_count", ctypes.c_int32), ("ltc0", ctypes.c_void_p), ("ltc1", ctypes.c_void_p),
                 ("ltc_width", ctypes.c_int32), ("ltc_height", ctypes.c_int32), ("ltc_layers", ctypes.c_int32),
                 ("ltc_constants", ctypes.c_float * 6), ("triangles", ctypes.c_void_p),
-                ("triangle_count", ctypes.c_int32), ("bvh_nodes", ctypes.c_void_p), ("bvh_node_count", ctypes.c_int32)]
+                ("triangle_count", ctypes.c_int32), ("bvh_nodes", ctypes.c_void_p), ("bvh_node_count", ctypes.c_int32),
+                ("cluster_offsets", ctypes.c_void_p), ("light_cluster", ctypes.c_void_p),
+                ("cluster_bounds", ctypes.c_void_p), ("cluster_power", ctypes.c_void_p),
+                ("cluster_count", ctypes.c_int32)]
 
 
 class Settings(ctypes.Structure):
@@ -31,7 +34,8 @@ class Settings(ctypes.Structure):
                 ("mis_heuristic", ctypes.c_int32), ("candidate_count", ctypes.c_int32),
                 ("sample_count", ctypes.c_int32), ("light_samples", ctypes.c_int32),
                 ("mis_visibility_estimate", ctypes.c_float), ("fast_atan", ctypes.c_int32),
-                ("reference_slots", ctypes.c_int32)]
+                ("reference_slots", ctypes.c_int32), ("proposal", ctypes.c_int32),
+                ("proposal_uniform_fraction", ctypes.c_float), ("random_number_proposal", ctypes.c_uint32)]
 
 
 class GBuffer(ctypes.Structure):
@@ -92,6 +96,22 @@ class OracleScene:
             s.bvh_node_count = self.nodes.shape[0]
         self.struct = s
 
+    def set_clusters(self, offsets, bounds, power):
+        """Cluster structure for the proposal: offsets (count + 1), bounds
+        (count x 4: centre, radius) and power (count), as the product
+        computes them (risltc_cluster_summaries)."""
+        self.offsets = np.ascontiguousarray(offsets, np.uint32)
+        self.bounds = np.ascontiguousarray(bounds, np.float32)
+        self.power = np.ascontiguousarray(power, np.float32)
+        count = self.offsets.size - 1
+        self.light_cluster = np.repeat(np.arange(count, dtype=np.uint32), np.diff(self.offsets.astype(np.int64)))
+        s = self.struct
+        s.cluster_offsets = self.offsets.ctypes.data
+        s.light_cluster = self.light_cluster.ctypes.data
+        s.cluster_bounds = self.bounds.ctypes.data
+        s.cluster_power = self.power.ctypes.data
+        s.cluster_count = count
+
 
 def triangles_v0e1e2(tris9):
     """(v0, v1, v2) rows to the 12-float {v0, 0, v1 - v0, 0, v2 - v0, 0} layout."""
@@ -104,7 +124,8 @@ def triangles_v0e1e2(tris9):
 
 
 def make_settings(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", candidates=32, sample_count=1,
-                  light_samples=1, mis_visibility_estimate=0.5, fast_atan=False, reference_slots=False):
+                  light_samples=1, mis_visibility_estimate=0.5, fast_atan=False, reference_slots=False,
+                  proposal=False, proposal_uniform_fraction=0.1, random_number_proposal=0):
     s = Settings()
     s.polygon_sampling_technique = TECHNIQUE[technique]
     s.light_sampling = LIGHT_SAMPLING[light_sampling]
@@ -115,6 +136,9 @@ def make_settings(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped
     s.mis_visibility_estimate = mis_visibility_estimate
     s.fast_atan = int(fast_atan)
     s.reference_slots = int(reference_slots)
+    s.proposal = int(proposal)
+    s.proposal_uniform_fraction = proposal_uniform_fraction
+    s.random_number_proposal = random_number_proposal
     return s
 
 

@@ -1059,9 +1059,107 @@ static vec3_t area_turk_shade(const ctx_t* c, const shading_data_t* sd, const li
 	return v3_scale(result, RC(1.0) / (R) st->sample_count);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Cluster proposal of the RIS candidates.  Not in the reference (which draws
+   candidates uniformly, shading_pass.frag.glsl:728-733): restates the CUDA
+   path's proposal_kernel in FP32 whatever R is, including the order of its
+   warp-wide sums (32 lanes, each summing a block of clusters, then an
+   inclusive Hillis-Steele scan over the lanes). */
+#define OR_MAX_CLUSTERS 1024
+#define OR_MAX_CANDIDATES 4096
+typedef struct {
+	int32_t light;
+	float pdf;
+} proposal_candidate_t;
+
+static float noise_f32(uint32_t* seed) {
+	*seed = 1664525u * *seed + 1013904223u;
+	return (float) *seed * 2.3283064365386962890625e-10f;
+}
+
+/* cluster_weight: power times a cosine bound over the clamped distance cubed */
+static float cluster_weight_f32(const float* bound, float power, const float* x, const float* n) {
+	const float v0 = bound[0] - x[0], v1 = bound[1] - x[1], v2 = bound[2] - x[2];
+	const float d2 = v0 * v0 + v1 * v1 + v2 * v2;
+	const float h = n[0] * v0 + n[1] * v1 + n[2] * v2;
+	const float rr = bound[3] * bound[3];
+	const float dd = d2 > rr ? d2 : rr;
+	float up = h + bound[3];
+	up = up > 0.0f ? up : 0.0f;
+	return (power * up) / (dd * sqrtf(dd));
+}
+
+static void proposal_draw(const oracle_scene_t* s, const oracle_settings_t* st, const float* x, const float* n,
+                          uint32_t px, uint32_t py, uint32_t width, proposal_candidate_t* out) {
+	const int k_count = s->cluster_count, n_lights = s->light_count;
+	const int per_lane = (k_count + 31) / 32;
+	const float a = st->proposal_uniform_fraction;
+	float cdf[OR_MAX_CLUSTERS], incl[32], next[32];
+	for (int lane = 0; lane != 32; ++lane) {
+		float local = 0.0f;
+		for (int j = 0; j != per_lane; ++j) {
+			const int k = lane * per_lane + j;
+			if (k >= k_count) break;
+			const int empty = s->cluster_offsets[k + 1] == s->cluster_offsets[k];
+			const float w = empty ? 0.0f : cluster_weight_f32(s->cluster_bounds + 4 * k, s->cluster_power[k], x, n);
+			local += w;
+			cdf[k] = local;
+		}
+		incl[lane] = local;
+	}
+	for (int d = 1; d < 32; d <<= 1) {
+		for (int l = 0; l != 32; ++l) next[l] = (l >= d) ? incl[l] + incl[l - d] : incl[l];
+		for (int l = 0; l != 32; ++l) incl[l] = next[l];
+	}
+	const float total = incl[31];
+	for (int lane = 0; lane != 32; ++lane) {
+		const float excl = lane == 0 ? 0.0f : incl[lane - 1];
+		for (int j = 0; j != per_lane; ++j) {
+			const int k = lane * per_lane + j;
+			if (k >= k_count) break;
+			cdf[k] = excl + cdf[k];
+		}
+	}
+	const int proposal = total > 0.0f && total <= 3.0e38f;
+	const uint32_t base = get_noise_accessor(px, py, width, st->random_number_proposal);
+	for (int c = 0; c != st->candidate_count; ++c) {
+		uint32_t sd = base ^ ((uint32_t) c * 0x9E3779B9u);
+		const float u0 = noise_f32(&sd), u1 = noise_f32(&sd), u2 = noise_f32(&sd);
+		int light;
+		if (!proposal || u0 < a) {
+			light = (int) (u1 * (float) n_lights);
+			if (light > n_lights - 1) light = n_lights - 1;
+		} else {
+			const float t = u1 * total;
+			int lo = 0, hi = k_count - 1;
+			while (lo < hi) {
+				const int mid = (lo + hi) >> 1;
+				if (cdf[mid] > t)
+					hi = mid;
+				else
+					lo = mid + 1;
+			}
+			while (lo > 0 && s->cluster_offsets[lo + 1] == s->cluster_offsets[lo]) --lo;
+			const uint32_t first = s->cluster_offsets[lo], size = s->cluster_offsets[lo + 1] - first;
+			uint32_t j = (uint32_t) (u2 * (float) size);
+			if (j > size - 1) j = size - 1;
+			light = (int) (first + j);
+		}
+		float pdf = 1.0f / (float) n_lights;
+		if (proposal) {
+			const uint32_t k = s->light_cluster[light];
+			const float mass = cdf[k] - (k > 0 ? cdf[k - 1] : 0.0f);
+			const uint32_t size = s->cluster_offsets[k + 1] - s->cluster_offsets[k];
+			pdf = a / (float) n_lights + ((1.0f - a) * (mass / total)) / (float) size;
+		}
+		out[c].light = light;
+		out[c].pdf = pdf;
+	}
+}
+
 /* Per-pixel body of the shading pass, shading_pass.frag.glsl:674-770 */
 static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed, R out_rgb[3],
-                        oracle_reservoir_t* out_res) {
+                        oracle_reservoir_t* out_res, const proposal_candidate_t* candidates) {
 	const oracle_settings_t* st = c->settings;
 	const oracle_scene_t* s = c->scene;
 	int n = s->light_count;
@@ -1103,6 +1201,11 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 			for (int i = 0; i != m; ++i) {
 				int light_idx = (int) (get_noise_1(&seed) * (R) n);
 				if (light_idx > n - 1) light_idx = n - 1;
+				R p = RC(1.0) / (R) n;
+				if (candidates) {
+					light_idx = candidates[i].light;
+					p = (R) candidates[i].pdf;
+				}
 				light_t l;
 				load_light(s, light_idx, &l);
 				vec3_t color;
@@ -1115,7 +1218,6 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 					color = psa_mis_shade(c, sd, ltc, &l, &seed, 0, 0);
 				}
 				R p_hat = v3_length(color);
-				R p = RC(1.0) / (R) n;
 				R w = p_hat / p;
 				/* insert_in_reservoir, reservoir.glsl:34-41 */
 				R rnd = get_noise_1(&seed);
@@ -1193,7 +1295,16 @@ int OR_EXPORT(oracle_render)(const oracle_scene_t* scene, const oracle_settings_
 				sd.fresnel_0 = V3((R) g[13 * np + i], (R) g[14 * np + i], (R) g[15 * np + i]);
 				sd.roughness = (R) g[16 * np + i];
 				uint32_t seed = get_noise_accessor((uint32_t) x, (uint32_t) y, (uint32_t) gbuffer->width, random_number_x);
-				shade_pixel(&c, &sd, seed, rgb, res);
+				proposal_candidate_t candidates[OR_MAX_CANDIDATES];
+				const int proposal = settings->proposal && settings->light_sampling == ORACLE_LIGHT_RESERVOIR &&
+				                     scene->cluster_count > 0 && settings->candidate_count <= OR_MAX_CANDIDATES;
+				if (proposal) {
+					const float xp[3] = {g[0 * np + i], g[1 * np + i], g[2 * np + i]};
+					const float nn[3] = {g[3 * np + i], g[4 * np + i], g[5 * np + i]};
+					proposal_draw(scene, settings, xp, nn, (uint32_t) x, (uint32_t) y, (uint32_t) gbuffer->width,
+					              candidates);
+				}
+				shade_pixel(&c, &sd, seed, rgb, res, proposal ? candidates : NULL);
 			}
 			out_rgb[3 * i + 0] = (ORACLE_OUT_T) rgb[0];
 			out_rgb[3 * i + 1] = (ORACLE_OUT_T) rgb[1];

@@ -94,3 +94,17 @@ void oracle_f32_any_hit(const oracle_scene_t* s, const float* rays, uint32_t cou
 		hits[i] = (uint32_t) any_hit(s, V3(r[0], r[1], r[2]), V3(r[4], r[5], r[6]), r[3], r[7]);
 	}
 }
+
+/* The cluster proposal's candidates of one shading point (position x,
+   normal n, pixel px, py of a width-wide frame): settings->candidate_count
+   lights with their probabilities. */
+void oracle_f32_proposal(const oracle_scene_t* s, const oracle_settings_t* st, const float* x, const float* n,
+                         uint32_t px, uint32_t py, uint32_t width, int32_t* lights, float* pdfs) {
+	static proposal_candidate_t out[OR_MAX_CANDIDATES];
+	if (st->candidate_count > OR_MAX_CANDIDATES || s->cluster_count <= 0 || s->cluster_count > OR_MAX_CLUSTERS) return;
+	proposal_draw(s, st, x, n, px, py, width, out);
+	for (int c = 0; c != st->candidate_count; ++c) {
+		lights[c] = out[c].light;
+		pdfs[c] = out[c].pdf;
+	}
+}

@@ -58,7 +58,8 @@ class Settings(ctypes.Structure):
                 ("mis_heuristic", ctypes.c_int32), ("candidate_count", ctypes.c_uint32),
                 ("sample_count", ctypes.c_uint32), ("sample_count_light", ctypes.c_uint32),
                 ("mis_visibility_estimate", ctypes.c_float), ("fast_atan", ctypes.c_uint32),
-                ("shadows", ctypes.c_uint32), ("numerics", ctypes.c_int32)]
+                ("shadows", ctypes.c_uint32), ("numerics", ctypes.c_int32), ("proposal", ctypes.c_int32),
+                ("proposal_uniform_fraction", ctypes.c_float)]
 
 
 class GBuffer(ctypes.Structure):
@@ -111,6 +112,8 @@ SIGNATURES = {
     "risltc_destroy_lights": (None, [ctypes.POINTER(PolygonalLight), ctypes.c_uint32]),
     "risltc_cluster_lights": (ctypes.c_int, [c_float_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
                                              ctypes.c_uint32, c_u32_p, c_u32_p]),
+    "risltc_cluster_summaries": (ctypes.c_int, [c_float_p, ctypes.c_uint32, ctypes.c_uint32, c_u32_p,
+                                                ctypes.c_uint32, c_float_p, c_float_p]),
     "risltc_default_settings": (None, [ctypes.POINTER(Settings)]),
     "risltc_ctx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]),
     "risltc_ctx_destroy": (None, [ctypes.c_void_p]),
@@ -119,6 +122,7 @@ SIGNATURES = {
                                            ctypes.POINTER(LtcTable), c_float_p, ctypes.c_uint32,
                                            ctypes.POINTER(ctypes.c_void_p)]),
     "risltc_scene_destroy": (None, [ctypes.c_void_p]),
+    "risltc_scene_set_clusters": (ctypes.c_int, [ctypes.c_void_p, c_u32_p, ctypes.c_uint32]),
     "risltc_shade": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer),
                                     ctypes.POINTER(Settings), ctypes.POINTER(NoiseTable), ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

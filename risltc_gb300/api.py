@@ -19,10 +19,12 @@ TECHNIQUES = {"baseline": 0, "area_turk": 1, "projected_solid_angle": 2, "projec
 MIS_HEURISTICS = {"balance": 0, "power": 1, "weighted": 2, "optimal_clamped": 3, "optimal": 4}
 LIGHT_SAMPLING = {"uniform": 0, "ris": 1}
 NUMERICS = {"exact": 0, "fast": 1}
+PROPOSALS = {"uniform": 0, "clusters": 1, "learned": 2}
 
 
 def settings(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", candidates=32, sample_count=1,
-             light_samples=1, mis_visibility_estimate=0.5, fast_atan=False, shadows=True, numerics="exact"):
+             light_samples=1, mis_visibility_estimate=0.5, fast_atan=False, shadows=True, numerics="exact",
+             proposal="uniform", proposal_uniform_fraction=0.1):
     """risltc_settings_t; defaults are specify_default_render_settings
     (src/main.c:220-236) with the reference's hard-coded M = 32."""
     s = _native.Settings()
@@ -37,6 +39,8 @@ def settings(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", ca
     s.fast_atan = int(fast_atan)
     s.shadows = int(shadows)
     s.numerics = NUMERICS[numerics]
+    s.proposal = PROPOSALS[proposal]
+    s.proposal_uniform_fraction = proposal_uniform_fraction
     return s
 
 
@@ -122,6 +126,13 @@ class Scene:
     def from_host_scene(cls, ctx, hs, shadows=True):
         return cls(ctx, hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants,
                    hs.triangles if shadows else None)
+
+    def set_clusters(self, offsets):
+        """risltc_scene_set_clusters: the lights must be listed cluster by
+        cluster (scenes.cluster_lights)."""
+        off = np.ascontiguousarray(offsets, np.uint32)
+        check(self._lib.risltc_scene_set_clusters(self._h, off.ctypes.data_as(_native.c_u32_p), off.size - 1),
+              "risltc_scene_set_clusters")
 
     @property
     def handle(self):

@@ -1,5 +1,6 @@
 // api.cu - the device half of the C ABI in include/risltc.h: contexts,
 // scene upload, frame shading and shadow queries.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -8,6 +9,7 @@
 #include "ris_wavefront.cuh"
 
 namespace risltc {
+cudaError_t launch_proposal(const ProposalParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast);
 cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,
                                cudaStream_t stream, int grid);
@@ -27,6 +29,9 @@ struct risltc_ctx_s {
 	// Reservoir records between the candidate and shading kernels.
 	risltc::ReservoirRecord* d_records;
 	size_t record_capacity;
+	// Proposal candidates (light, pdf) per pixel-frame and candidate.
+	risltc::ProposalCandidate* d_candidates;
+	size_t candidate_capacity;
 	// The shading phase's state between its sample, shadow-ray and resolve
 	// kernels: a 64-byte sample record per pixel-frame, up to two 32-byte
 	// shadow rays per pixel-frame (as staged, then grouped by light), their
@@ -63,6 +68,12 @@ struct risltc_scene_s {
 	void* d_triangles;
 	uint32_t max_vertex_count;
 	uint32_t bvh_depth;
+	// Cluster structure of the lights (risltc_scene_set_clusters).
+	risltc::ClusterView clusters;
+	void* d_cluster_offsets;
+	void* d_light_cluster;
+	void* d_cluster_bounds;
+	void* d_cluster_power;
 };
 
 namespace {
@@ -226,6 +237,7 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFree(ctx->d_rgb);
 	cudaFreeHost(ctx->h_pinned_rgb);
 	cudaFree(ctx->d_records);
+	cudaFree(ctx->d_candidates);
 	cudaFree(ctx->d_samples);
 	cudaFree(ctx->d_staged);
 	cudaFree(ctx->d_rays);
@@ -348,7 +360,67 @@ EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene) {
 	cudaFree(scene->d_ltc);
 	cudaFree(scene->d_pairs);
 	cudaFree(scene->d_triangles);
+	cudaFree(scene->d_cluster_offsets);
+	cudaFree(scene->d_light_cluster);
+	cudaFree(scene->d_cluster_bounds);
+	cudaFree(scene->d_cluster_power);
 	free(scene);
+}
+
+EXTERN_C int risltc_scene_set_clusters(risltc_scene_t* scene, const uint32_t* offsets, uint32_t cluster_count) {
+	if (!scene || !offsets || cluster_count == 0 || cluster_count > (uint32_t) risltc::kMaxClusters)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	const uint32_t n = (uint32_t) scene->view.light_count;
+	if (offsets[0] != 0 || offsets[cluster_count] != n) return RISLTC_ERROR_INVALID_ARGUMENT;
+	for (uint32_t c = 0; c != cluster_count; ++c)
+		if (offsets[c + 1] < offsets[c]) return RISLTC_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(scene->ctx->device);
+	cudaStreamSynchronize(scene->ctx->stream);
+	// The device light records {radiance, count}, plane, 8 vertex slots, as
+	// std140 rows for risltc_cluster_summaries.
+	std::vector<float> rec((size_t) n * risltc::kLightWords);
+	cudaError_t e = cudaMemcpy(rec.data(), scene->d_lights, rec.size() * sizeof(float), cudaMemcpyDeviceToHost);
+	if (e != cudaSuccess) return cuda_status(e);
+	const uint32_t maxv = risltc::kMaxLightVertices;
+	const size_t stride = 12 + 4 * (size_t) maxv;
+	std::vector<float> std140(stride * n, 0.0f);
+	for (uint32_t l = 0; l != n; ++l) {
+		const float* r = &rec[(size_t) l * risltc::kLightWords];
+		float* row = &std140[stride * l];
+		for (int a = 0; a != 3; ++a) row[a] = r[a];
+		for (int a = 0; a != 4; ++a) row[4 + a] = r[4 + a];
+		memcpy(row + 8, r + 3, sizeof(float));
+		for (uint32_t v = 0; v != maxv; ++v)
+			for (int a = 0; a != 3; ++a) row[12 + 4 * v + a] = r[8 + 4 * v + a];
+	}
+	std::vector<float> bounds(4 * (size_t) cluster_count), power(cluster_count);
+	int st = risltc_cluster_summaries(std140.data(), n, maxv, offsets, cluster_count, bounds.data(), power.data());
+	if (st) return st;
+	std::vector<uint32_t> light_cluster(n);
+	for (uint32_t c = 0; c != cluster_count; ++c)
+		for (uint32_t l = offsets[c]; l != offsets[c + 1]; ++l) light_cluster[l] = c;
+	cudaFree(scene->d_cluster_offsets);
+	cudaFree(scene->d_light_cluster);
+	cudaFree(scene->d_cluster_bounds);
+	cudaFree(scene->d_cluster_power);
+	scene->d_cluster_offsets = scene->d_light_cluster = scene->d_cluster_bounds = scene->d_cluster_power = nullptr;
+	scene->clusters = risltc::ClusterView{};
+	auto upload = [&](void** dst, const void* src, size_t bytes) {
+		if (e != cudaSuccess) return;
+		e = cudaMalloc(dst, bytes);
+		if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+	};
+	upload(&scene->d_cluster_offsets, offsets, sizeof(uint32_t) * (cluster_count + 1));
+	upload(&scene->d_light_cluster, light_cluster.data(), sizeof(uint32_t) * n);
+	upload(&scene->d_cluster_bounds, bounds.data(), sizeof(float) * bounds.size());
+	upload(&scene->d_cluster_power, power.data(), sizeof(float) * power.size());
+	if (e != cudaSuccess) return cuda_status(e);
+	scene->clusters.offsets = (const uint32_t*) scene->d_cluster_offsets;
+	scene->clusters.light_cluster = (const uint32_t*) scene->d_light_cluster;
+	scene->clusters.bounds = (const float4*) scene->d_cluster_bounds;
+	scene->clusters.power = (const float*) scene->d_cluster_power;
+	scene->clusters.count = (int) cluster_count;
+	return RISLTC_OK;
 }
 
 static int validate_settings(const risltc_settings_t* s) {
@@ -364,6 +436,17 @@ static int validate_settings(const risltc_settings_t* s) {
 	    s->sample_count_light < 1 || s->sample_count_light > 64)
 		return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (s->numerics != risltc_numerics_exact && s->numerics != risltc_numerics_fast) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (s->proposal != risltc_proposal_uniform && s->proposal != risltc_proposal_clusters &&
+	    s->proposal != risltc_proposal_learned)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (s->proposal != risltc_proposal_uniform) {
+		if (!(s->proposal_uniform_fraction > 0.0f && s->proposal_uniform_fraction <= 1.0f))
+			return RISLTC_ERROR_INVALID_ARGUMENT;
+		// Proposals feed the RIS candidates of the default configuration.
+		if (s->polygon_sampling_technique != sample_polygon_ltc_cp || s->light_sampling != light_reservoir ||
+		    s->sample_count_light != 1)
+			return RISLTC_ERROR_UNSUPPORTED;
+	}
 	return RISLTC_OK;
 }
 
@@ -390,6 +473,7 @@ bool uses_ray_queue(const risltc_scene_t* scene, const risltc_settings_t* s, siz
 // One call's share of the context's scratch.
 struct Scratch {
 	risltc::ReservoirRecord* records;
+	risltc::ProposalCandidate* candidates;
 	risltc::SampleRecord* samples;
 	risltc::ShadowRay* staged;
 	risltc::ShadowRay* rays;
@@ -397,6 +481,21 @@ struct Scratch {
 	uint32_t* ray_count;
 	uint32_t* light_rays;
 };
+
+bool uses_proposal(const risltc_settings_t* s) { return s->proposal != risltc_proposal_uniform; }
+
+int reserve_candidates(risltc_ctx_t* ctx, size_t need) {
+	if (need <= ctx->candidate_capacity) return RISLTC_OK;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_candidates);
+	ctx->d_candidates = nullptr;
+	ctx->candidate_capacity = 0;
+	cudaError_t e = cudaMalloc(&ctx->d_candidates, need * sizeof(risltc::ProposalCandidate));
+	if (e != cudaSuccess) return cuda_status(e);
+	ctx->candidate_capacity = need;
+	return RISLTC_OK;
+}
 
 int reserve_records(risltc_ctx_t* ctx, size_t need) {
 	if (need <= ctx->record_capacity) return RISLTC_OK;
@@ -442,6 +541,26 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 	const size_t pixels = (size_t) gbuffer->width * gbuffer->height;
 	const bool fast = settings->numerics == risltc_numerics_fast;
 	cudaError_t e;
+	if (uses_proposal(settings)) {
+		risltc::ProposalParams q;
+		memset(&q, 0, sizeof(q));
+		q.scene = scene->view;
+		q.clusters = scene->clusters;
+		q.gbuffer = gbuffer->planes;
+		q.primitive = gbuffer->primitive;
+		q.width = gbuffer->width;
+		q.height = gbuffer->height;
+		q.candidate_count = (int) settings->candidate_count;
+		q.noise_seed = noise_seed;
+		q.animate = animate;
+		q.frame_count = frame_count;
+		q.uniform_fraction = settings->proposal_uniform_fraction;
+		q.logits = nullptr;
+		q.out = sc.candidates;
+		const int warps = (int) ((pixels + risltc::kProposalWarps - 1) / risltc::kProposalWarps);
+		e = risltc::launch_proposal(q, stream, std::min(warps, ctx->sm_count * 16));
+		if (e != cudaSuccess) return cuda_status(e);
+	}
 	if (uses_ris_pipeline(settings)) {
 		// The reference's default configuration: candidate and shading
 		// kernels with reservoir records in between.
@@ -462,6 +581,7 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		r.animate = p.animate;
 		r.frame_count = p.frame_count;
 		r.records = sc.records;
+		r.candidates = uses_proposal(settings) ? sc.candidates : nullptr;
 		if (uses_ray_queue(scene, settings, pixels * frame_count)) {
 			r.samples = sc.samples;
 			r.staged = sc.staged;
@@ -490,8 +610,12 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 	if (!ctx || !valid_call(scene, gbuffer, noise, frame_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	int st = validate_settings(settings);
 	if (st) return st;
+	if (settings->proposal == risltc_proposal_learned) return RISLTC_ERROR_UNSUPPORTED;
+	if (uses_proposal(settings) && scene->clusters.count == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
 	cudaSetDevice(ctx->device);
 	const size_t pixel_frames = (size_t) gbuffer->width * gbuffer->height * frame_count;
+	if (uses_proposal(settings) && (st = reserve_candidates(ctx, pixel_frames * settings->candidate_count)))
+		return st;
 	if (uses_ris_pipeline(settings)) {
 		if ((st = reserve_records(ctx, pixel_frames))) return st;
 		if (uses_ray_queue(scene, settings, pixel_frames) &&
@@ -507,8 +631,8 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		}
 		events = ctx->events[i];
 	}
-	const Scratch sc{ctx->d_records, ctx->d_samples, ctx->d_staged, ctx->d_rays, ctx->d_hits, ctx->d_ray_count,
-	                 ctx->d_light_rays};
+	const Scratch sc{ctx->d_records, ctx->d_candidates, ctx->d_samples, ctx->d_staged, ctx->d_rays, ctx->d_hits,
+	                 ctx->d_ray_count, ctx->d_light_rays};
 	st = shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise->random_seed, animate, frame_count, out_rgb,
 	               accum, reservoirs, events);
 	if (st) return st;
@@ -520,14 +644,17 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	if (!ctx || (!items && item_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (item_count == 0) return RISLTC_OK;
 	// Validate everything before any work; size the scratch for all items.
-	size_t records = 0, wavefront = 0, lights = 0, queues = 0;
+	size_t records = 0, wavefront = 0, lights = 0, queues = 0, candidates = 0;
 	for (uint32_t i = 0; i != item_count; ++i) {
 		const risltc_batch_item_t& it = items[i];
 		if (!valid_call(it.scene, &it.gbuffer, it.noise, it.frame_count) || it.scene->ctx != ctx)
 			return RISLTC_ERROR_INVALID_ARGUMENT;
 		int st = validate_settings(&it.settings);
 		if (st) return st;
+		if (it.settings.proposal == risltc_proposal_learned) return RISLTC_ERROR_UNSUPPORTED;
+		if (uses_proposal(&it.settings) && it.scene->clusters.count == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
 		const size_t pf = (size_t) it.gbuffer.width * it.gbuffer.height * it.frame_count;
+		if (uses_proposal(&it.settings)) candidates += pf * it.settings.candidate_count;
 		if (uses_ris_pipeline(&it.settings)) records += pf;
 		if (uses_ray_queue(it.scene, &it.settings, pf)) {
 			wavefront += pf;
@@ -538,6 +665,7 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	cudaSetDevice(ctx->device);
 	int st;
 	if (records && (st = reserve_records(ctx, records))) return st;
+	if (candidates && (st = reserve_candidates(ctx, candidates))) return st;
 	if (queues && (st = reserve_wavefront(ctx, wavefront, lights, queues))) return st;
 	cudaError_t e = cudaSuccess;
 	if (!ctx->batch_streams_created) {
@@ -554,7 +682,7 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	if ((e = cudaEventRecord(ctx->batch_fork, ctx->stream)) != cudaSuccess) return cuda_status(e);
 	for (int k = 0; k != streams; ++k)
 		if ((e = cudaStreamWaitEvent(ctx->batch_streams[k], ctx->batch_fork, 0)) != cudaSuccess) return cuda_status(e);
-	size_t r_off = 0, w_off = 0, l_off = 0, q_off = 0;
+	size_t r_off = 0, w_off = 0, l_off = 0, q_off = 0, c_off = 0;
 	for (uint32_t i = 0; i != item_count; ++i) {
 		const risltc_batch_item_t& it = items[i];
 		const size_t pf = (size_t) it.gbuffer.width * it.gbuffer.height * it.frame_count;
@@ -562,6 +690,10 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 		if (uses_ris_pipeline(&it.settings)) {
 			sc.records = ctx->d_records + r_off;
 			r_off += pf;
+		}
+		if (uses_proposal(&it.settings)) {
+			sc.candidates = ctx->d_candidates + c_off;
+			c_off += pf * it.settings.candidate_count;
 		}
 		if (uses_ray_queue(it.scene, &it.settings, pf)) {
 			sc.samples = ctx->d_samples + w_off;

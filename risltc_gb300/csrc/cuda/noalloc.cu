@@ -49,7 +49,7 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 	    gbuffer->height == 0)
 		return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (settings->polygon_sampling_technique != sample_polygon_ltc_cp || settings->light_sampling != light_reservoir ||
-	    settings->sample_count_light != 1)
+	    settings->sample_count_light != 1 || settings->proposal != risltc_proposal_uniform)
 		return RISLTC_ERROR_UNSUPPORTED;
 	if (settings->candidate_count < 1 || settings->candidate_count > 4096 || settings->sample_count < 1 ||
 	    settings->sample_count > 64 || (int) settings->mis_heuristic < 0 ||

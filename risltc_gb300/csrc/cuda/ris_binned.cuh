@@ -253,6 +253,8 @@ ris_candidates_binned_kernel(RisParams pr) {
 						if (valid && k < chunk) {
 							int idx = (int) (get_noise_1(draw) * (float) n_lights);
 							idx = idx > n_lights - 1 ? n_lights - 1 : idx;
+							if (pr.candidates)
+								idx = pr.candidates[((size_t) f * np + i) * pr.candidate_count + cs + c0 + k].light;
 							get_noise_1(draw);
 							light[k] = idx;
 							bin[k] = __float_as_uint(__ldg(light_record(pr.scene, idx)).w) - 3u;
@@ -338,9 +340,16 @@ ris_candidates_binned_kernel(RisParams pr) {
 					for (int k = 0; k < super_count; ++k) {
 						int idx = (int) (get_noise_1(seed) * (float) n_lights);
 						idx = idx > n_lights - 1 ? n_lights - 1 : idx;
+						float pk = p;
+						if (pr.candidates) {
+							const ProposalCandidate q =
+							    pr.candidates[((size_t) f * np + i) * pr.candidate_count + cs + k];
+							idx = q.light;
+							pk = q.pdf;
+						}
 						const float rnd = get_noise_1(seed);
 						const float p_hat = tile.p_hat[lane * kSuper + k];
-						const float w = P::div(p_hat, p);
+						const float w = P::div(p_hat, pk);
 						w_sum += w;
 						if (w > 0.0f && rnd < P::div(w, w_sum)) {
 							res_index = idx;

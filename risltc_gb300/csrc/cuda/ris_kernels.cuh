@@ -12,6 +12,7 @@
 // small.  Results are bit-identical to the fused kernel (same operations in
 // the same order).
 #pragma once
+#include "proposal.cuh"
 #include "shade_kernel.cuh"
 
 namespace risltc {
@@ -38,6 +39,9 @@ struct RisParams {
 	uint32_t animate;
 	uint32_t frame_count;
 	ReservoirRecord* records;  // [frame][pixel] scratch
+	// Candidates drawn by a proposal ([frame][pixel][candidate]); null: each
+	// candidate is drawn uniformly from the pixel's noise as in the reference.
+	const ProposalCandidate* candidates;
 	// Shadow rays traced in their own pass (null: traced in ris_shade_kernel).
 	struct SampleRecord* samples;  // [frame][pixel]
 	struct ShadowRay* staged;      // [frame][pixel][technique], as generated
@@ -188,6 +192,12 @@ __global__ void __launch_bounds__(128, RISLTC_CANDIDATE_MIN_BLOCKS) ris_candidat
 			for (int c = 0; c != pr.candidate_count; ++c) {
 				int idx = (int) (get_noise_1(seed) * (float) n);
 				idx = idx > n - 1 ? n - 1 : idx;
+				float pc = p;
+				if (pr.candidates) {
+					const ProposalCandidate q = pr.candidates[((size_t) f * np + i) * pr.candidate_count + c];
+					idx = q.light;
+					pc = q.pdf;
+				}
 				{
 					// The next candidate's index is two LCG steps ahead: start
 					// pulling its record (two cache lines) into L1 now.
@@ -200,7 +210,7 @@ __global__ void __launch_bounds__(128, RISLTC_CANDIDATE_MIN_BLOCKS) ris_candidat
 				}
 				f3 color = ltc_cp_candidate<P>(cf, light_record(pr.scene, idx));
 				float p_hat = P::sqrt(dot(color, color));
-				float w = P::div(p_hat, p);
+				float w = P::div(p_hat, pc);
 				float rnd = get_noise_1(seed);
 				w_sum += w;
 				if (w > 0.0f && rnd < P::div(w, w_sum)) {

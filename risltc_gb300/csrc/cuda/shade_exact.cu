@@ -29,6 +29,10 @@ cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid) 
 	ris_shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
 	return cudaGetLastError();
 }
+cudaError_t launch_proposal(const ProposalParams& p, cudaStream_t stream, int grid) {
+	proposal_kernel<<<grid, 32 * kProposalWarps, proposal_smem_bytes(p.clusters.count), stream>>>(p);
+	return cudaGetLastError();
+}
 cudaError_t launch_ris_sample(const RisParams& p, cudaStream_t stream, int grid) {
 	ris_sample_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
 	return cudaGetLastError();

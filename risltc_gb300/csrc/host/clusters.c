@@ -112,3 +112,62 @@ int risltc_cluster_lights(const float* centers, uint32_t light_count, uint32_t c
 	free(label);
 	return RISLTC_OK;
 }
+
+int risltc_cluster_summaries(const float* lights_std140, uint32_t light_count, uint32_t max_vertex_count,
+                             const uint32_t* offsets, uint32_t cluster_count, float* bounds, float* power) {
+	if (!lights_std140 || !offsets || !bounds || !power || cluster_count == 0 || max_vertex_count < 3 ||
+	    offsets[0] != 0 || offsets[cluster_count] != light_count)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	const size_t stride = 12 + 4 * (size_t) max_vertex_count;
+	for (uint32_t c = 0; c != cluster_count; ++c)
+		if (offsets[c + 1] < offsets[c]) return RISLTC_ERROR_INVALID_ARGUMENT;
+	for (uint32_t c = 0; c != cluster_count; ++c) {
+		double centre[3] = {0.0, 0.0, 0.0}, radius = 0.0, watts = 0.0;
+		uint32_t count = 0;
+		for (uint32_t l = offsets[c]; l != offsets[c + 1]; ++l) {
+			const float* row = lights_std140 + stride * l;
+			uint32_t nv;
+			memcpy(&nv, row + 8, sizeof(nv));
+			if (nv > max_vertex_count) return RISLTC_ERROR_VERTEX_COUNT;
+			const float* v = row + 12;
+			for (uint32_t i = 0; i != nv; ++i)
+				for (int a = 0; a != 3; ++a) centre[a] += v[4 * i + a];
+			count += nv;
+			/* Area by a fan from vertex 0; luminance of the radiance. */
+			double area = 0.0;
+			for (uint32_t i = 1; i + 1 < nv; ++i) {
+				double e1[3], e2[3];
+				for (int a = 0; a != 3; ++a) {
+					e1[a] = (double) v[4 * i + a] - v[a];
+					e2[a] = (double) v[4 * (i + 1) + a] - v[a];
+				}
+				const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+				             cz = e1[0] * e2[1] - e1[1] * e2[0];
+				area += 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+			}
+			watts += (0.2126 * row[0] + 0.7152 * row[1] + 0.0722 * row[2]) * area;
+		}
+		if (count)
+			for (int a = 0; a != 3; ++a) centre[a] /= count;
+		for (int a = 0; a != 3; ++a) bounds[4 * c + a] = (float) centre[a];
+		for (uint32_t l = offsets[c]; l != offsets[c + 1]; ++l) {
+			const float* row = lights_std140 + stride * l;
+			uint32_t nv;
+			memcpy(&nv, row + 8, sizeof(nv));
+			for (uint32_t i = 0; i != nv; ++i) {
+				/* Distance to the stored (float) centre, so the sphere holds
+				   the vertices around the centre the kernels use. */
+				double d2 = 0.0;
+				for (int a = 0; a != 3; ++a) {
+					const double d = (double) row[12 + 4 * i + a] - (double) bounds[4 * c + a];
+					d2 += d * d;
+				}
+				if (sqrt(d2) > radius) radius = sqrt(d2);
+			}
+		}
+		/* Rounded up so that the sphere still holds every vertex. */
+		bounds[4 * c + 3] = nextafterf((float) radius, INFINITY);
+		power[c] = (float) watts;
+	}
+	return RISLTC_OK;
+}

@@ -166,4 +166,6 @@ void risltc_default_settings(risltc_settings_t* s) {
 	s->fast_atan = 0;
 	s->shadows = 1;
 	s->numerics = risltc_numerics_exact;
+	s->proposal = risltc_proposal_uniform;
+	s->proposal_uniform_fraction = 0.1f;
 }

@@ -145,18 +145,40 @@ def light_centers(lights_std140):
     return ((verts * mask[:, :, None]).sum(1) / n[:, None]).astype(np.float32)
 
 
-def cluster_lights(hs, cluster_count, seed=0, iterations=32):
-    """risltc_cluster_lights on the scene's light centres.  Returns a copy of
-    the scene with its lights (and light specs) listed cluster by cluster, and
-    the cluster offsets (cluster c holds lights offsets[c] .. offsets[c + 1])."""
+def cluster_order(lights_std140, cluster_count, seed=0, iterations=32):
+    """risltc_cluster_lights on the lights' centres: (order, offsets)."""
     lib = _native.load()
-    centers = np.ascontiguousarray(light_centers(hs.lights))
+    centers = np.ascontiguousarray(light_centers(lights_std140))
     n = centers.shape[0]
     order = np.zeros(n, np.uint32)
     offsets = np.zeros(cluster_count + 1, np.uint32)
     _native.check(lib.risltc_cluster_lights(centers.ctypes.data_as(_native.c_float_p), n, cluster_count, seed,
                                             iterations, order.ctypes.data_as(_native.c_u32_p),
                                             offsets.ctypes.data_as(_native.c_u32_p)), "risltc_cluster_lights")
+    return order, offsets
+
+
+def cluster_summaries(lights_std140, max_vertex_count, offsets):
+    """risltc_cluster_summaries: (bounds [K, 4], power [K]) of lights listed
+    cluster by cluster."""
+    lib = _native.load()
+    lights = np.ascontiguousarray(lights_std140, np.float32)
+    offsets = np.ascontiguousarray(offsets, np.uint32)
+    k = offsets.size - 1
+    bounds = np.zeros((k, 4), np.float32)
+    power = np.zeros(k, np.float32)
+    _native.check(lib.risltc_cluster_summaries(lights.ctypes.data_as(_native.c_float_p), lights.shape[0],
+                                               max_vertex_count, offsets.ctypes.data_as(_native.c_u32_p), k,
+                                               bounds.ctypes.data_as(_native.c_float_p),
+                                               power.ctypes.data_as(_native.c_float_p)), "risltc_cluster_summaries")
+    return bounds, power
+
+
+def cluster_lights(hs, cluster_count, seed=0, iterations=32):
+    """A copy of the scene with its lights (and light specs) listed cluster by
+    cluster, and the cluster offsets (cluster c holds lights offsets[c] ..
+    offsets[c + 1])."""
+    order, offsets = cluster_order(hs.lights, cluster_count, seed, iterations)
     specs = [hs.light_specs[i] for i in order] if hs.light_specs else []
     out = HostScene(hs.width, hs.height, hs.gbuffer, hs.primitive, np.ascontiguousarray(hs.lights[order]),
                     hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants, hs.triangles, specs)
