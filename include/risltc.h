@@ -317,6 +317,7 @@ typedef struct risltc_reservoir_s {
 
 typedef struct risltc_ctx_s risltc_ctx_t;
 typedef struct risltc_scene_s risltc_scene_t;
+typedef struct risltc_model_s risltc_model_t;
 
 /* stream: a cudaStream_t, or NULL for the legacy default stream. */
 EXTERN_C int risltc_ctx_create(risltc_ctx_t** ctx, int device, void* stream);
@@ -329,6 +330,31 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx);
    clusters).  Derives each cluster's bounding sphere and power (luminance x
    area summed over its lights) and uploads them. */
 EXTERN_C int risltc_scene_set_clusters(risltc_scene_t* scene, const uint32_t* offsets, uint32_t cluster_count);
+
+/* The learned cluster proposal (no counterpart in the reference): an MLP
+   from a shading point's position (centred and scaled by the model's input
+   transform), normal, outgoing direction and roughness, encoded with six
+   sine/cosine frequencies per input (144 features), through two hidden
+   layers of 64 ReLU units to one logit per cluster; BF16 weights, FP32
+   accumulation on the tensor cores.  q(cluster) = softmax(logits).
+   Parameters: FP32, in the order W1 [64][144], b1 [64], W2 [64][64], b2 [64],
+   W3 [clusters][64], b3 [clusters] (risltc_model_parameter_count floats). */
+EXTERN_C uint32_t risltc_model_parameter_count(uint32_t cluster_count);
+/* cluster_count: a multiple of 8, at most 1024.  Weights He-uniform from the
+   seed (the output layer scaled by 0.1), biases zero. */
+EXTERN_C int risltc_model_create(risltc_ctx_t* ctx, uint32_t cluster_count, uint64_t seed, risltc_model_t** model);
+EXTERN_C void risltc_model_destroy(risltc_model_t* model);
+EXTERN_C int risltc_model_set_params(risltc_model_t* model, const float* params);
+EXTERN_C int risltc_model_get_params(const risltc_model_t* model, float* params);
+/* Inputs: position (p - center) / half_extent. */
+EXTERN_C int risltc_model_set_input_transform(risltc_model_t* model, const float center[3], float half_extent);
+/* The model the scene's learned proposal uses (its cluster count must match
+   the scene's clusters); NULL detaches.  The scene does not own it. */
+EXTERN_C int risltc_scene_set_model(risltc_scene_t* scene, risltc_model_t* model);
+/* The model's logits for every pixel of the G-buffer (device pointers;
+   logits: width * height * cluster_count floats, pixel-major), stream-ordered. */
+EXTERN_C int risltc_model_logits(risltc_ctx_t* ctx, const risltc_model_t* model, const risltc_gbuffer_t* gbuffer,
+                                 float* logits);
 
 /* Uploads lights (the std140 buffer of risltc_write_lights), the LTC table
    and, if triangle_count > 0, builds and uploads the BVH of the occluders

@@ -114,6 +114,15 @@ SIGNATURES = {
                                              ctypes.c_uint32, c_u32_p, c_u32_p]),
     "risltc_cluster_summaries": (ctypes.c_int, [c_float_p, ctypes.c_uint32, ctypes.c_uint32, c_u32_p,
                                                 ctypes.c_uint32, c_float_p, c_float_p]),
+    "risltc_model_parameter_count": (ctypes.c_uint32, [ctypes.c_uint32]),
+    "risltc_model_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "risltc_model_destroy": (None, [ctypes.c_void_p]),
+    "risltc_model_set_params": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
+    "risltc_model_get_params": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
+    "risltc_model_set_input_transform": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_float]),
+    "risltc_scene_set_model": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "risltc_model_logits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer), ctypes.c_void_p]),
     "risltc_default_settings": (None, [ctypes.POINTER(Settings)]),
     "risltc_ctx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]),
     "risltc_ctx_destroy": (None, [ctypes.c_void_p]),

@@ -127,6 +127,11 @@ class Scene:
         return cls(ctx, hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants,
                    hs.triangles if shadows else None)
 
+    def set_model(self, model):
+        """risltc_scene_set_model (None detaches)."""
+        check(self._lib.risltc_scene_set_model(self._h, None if model is None else model.handle),
+              "risltc_scene_set_model")
+
     def set_clusters(self, offsets):
         """risltc_scene_set_clusters: the lights must be listed cluster by
         cluster (scenes.cluster_lights)."""
@@ -141,6 +146,63 @@ class Scene:
     def close(self):
         if self._h:
             self._lib.risltc_scene_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+class Model:
+    """risltc_model_t: the learned cluster proposal's MLP (see include/risltc.h)."""
+
+    def __init__(self, ctx, cluster_count, seed=0):
+        self._lib = _native.load()
+        self.ctx = ctx
+        self.cluster_count = cluster_count
+        self._h = ctypes.c_void_p()
+        check(self._lib.risltc_model_create(ctx.handle, cluster_count, seed, ctypes.byref(self._h)),
+              "risltc_model_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def parameter_count(self):
+        return int(self._lib.risltc_model_parameter_count(self.cluster_count))
+
+    def get_params(self):
+        out = np.zeros(self.parameter_count, np.float32)
+        check(self._lib.risltc_model_get_params(self._h, out.ctypes.data_as(_native.c_float_p)),
+              "risltc_model_get_params")
+        return out
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == self.parameter_count
+        check(self._lib.risltc_model_set_params(self._h, p.ctypes.data_as(_native.c_float_p)),
+              "risltc_model_set_params")
+
+    def set_input_transform(self, center, half_extent):
+        c = np.ascontiguousarray(center, np.float32)
+        check(self._lib.risltc_model_set_input_transform(self._h, c.ctypes.data_as(_native.c_float_p),
+                                                         float(half_extent)), "risltc_model_set_input_transform")
+
+    def logits(self, gbuffer, width, height, primitive=None):
+        """Device tensor [width*height, clusters] of the model's logits."""
+        import torch
+        out = torch.empty((width * height, self.cluster_count), dtype=torch.float32, device=gbuffer.device)
+        g = _native.GBuffer(width, height, gbuffer.data_ptr(), None if primitive is None else primitive.data_ptr())
+        check(self._lib.risltc_model_logits(self.ctx.handle, self._h, ctypes.byref(g), ctypes.c_void_p(out.data_ptr())),
+              "risltc_model_logits")
+        return out
+
+    def close(self):
+        if self._h:
+            self._lib.risltc_model_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

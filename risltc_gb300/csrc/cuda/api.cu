@@ -1,11 +1,13 @@
 // api.cu - the device half of the C ABI in include/risltc.h: contexts,
 // scene upload, frame shading and shadow queries.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
 #include <cuda_runtime.h>
+#include "mlp.cuh"
 #include "ris_wavefront.cuh"
 
 namespace risltc {
@@ -32,6 +34,9 @@ struct risltc_ctx_s {
 	// Proposal candidates (light, pdf) per pixel-frame and candidate.
 	risltc::ProposalCandidate* d_candidates;
 	size_t candidate_capacity;
+	// The learned proposal's logits (BF16) per pixel and cluster.
+	__nv_bfloat16* d_logits;
+	size_t logit_capacity;
 	// The shading phase's state between its sample, shadow-ray and resolve
 	// kernels: a 64-byte sample record per pixel-frame, up to two 32-byte
 	// shadow rays per pixel-frame (as staged, then grouped by light), their
@@ -74,6 +79,17 @@ struct risltc_scene_s {
 	void* d_light_cluster;
 	void* d_cluster_bounds;
 	void* d_cluster_power;
+	// The learned proposal's model (risltc_scene_set_model), not owned.
+	risltc_model_t* model;
+};
+
+struct risltc_model_s {
+	risltc_ctx_t* ctx;
+	int cluster_count;
+	int parameter_count;
+	float* d_params;             // FP32 parameters (risltc_model_parameter_count)
+	__nv_bfloat16* d_weights;    // their BF16 copy used by the kernels
+	float center[3], inv_half_extent;
 };
 
 namespace {
@@ -238,6 +254,7 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFreeHost(ctx->h_pinned_rgb);
 	cudaFree(ctx->d_records);
 	cudaFree(ctx->d_candidates);
+	cudaFree(ctx->d_logits);
 	cudaFree(ctx->d_samples);
 	cudaFree(ctx->d_staged);
 	cudaFree(ctx->d_rays);
@@ -474,6 +491,7 @@ bool uses_ray_queue(const risltc_scene_t* scene, const risltc_settings_t* s, siz
 struct Scratch {
 	risltc::ReservoirRecord* records;
 	risltc::ProposalCandidate* candidates;
+	__nv_bfloat16* logits;
 	risltc::SampleRecord* samples;
 	risltc::ShadowRay* staged;
 	risltc::ShadowRay* rays;
@@ -483,6 +501,49 @@ struct Scratch {
 };
 
 bool uses_proposal(const risltc_settings_t* s) { return s->proposal != risltc_proposal_uniform; }
+
+int reserve_logits(risltc_ctx_t* ctx, size_t need) {
+	if (need <= ctx->logit_capacity) return RISLTC_OK;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_logits);
+	ctx->d_logits = nullptr;
+	ctx->logit_capacity = 0;
+	cudaError_t e = cudaMalloc(&ctx->d_logits, need * sizeof(__nv_bfloat16));
+	if (e != cudaSuccess) return cuda_status(e);
+	ctx->logit_capacity = need;
+	return RISLTC_OK;
+}
+
+// The model's logits for every pixel of the G-buffer into logits.
+cudaError_t launch_logits(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_model_t* m,
+                          const risltc_gbuffer_t* gbuffer, __nv_bfloat16* logits) {
+	risltc::MlpParams q;
+	memset(&q, 0, sizeof(q));
+	q.gbuffer = gbuffer->planes;
+	q.primitive = gbuffer->primitive;
+	q.width = gbuffer->width;
+	q.height = gbuffer->height;
+	q.weights = m->d_weights;
+	q.params = m->d_params;
+	q.k_count = m->cluster_count;
+	for (int a = 0; a != 3; ++a) q.center[a] = m->center[a];
+	q.inv_half_extent = m->inv_half_extent;
+	q.logits = logits;
+	const size_t smem = risltc::mlp_smem_bytes(m->cluster_count);
+	static std::atomic<uint64_t> configured{0};
+	const uint64_t bit = 1ull << (ctx->device & 63);
+	if (!(configured.load() & bit)) {
+		cudaError_t e = cudaFuncSetAttribute(risltc::mlp_logits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                     (int) risltc::mlp_smem_bytes(risltc::kMaxClusters));
+		if (e != cudaSuccess) return e;
+		configured.fetch_or(bit);
+	}
+	const size_t tiles = ((size_t) gbuffer->width * gbuffer->height + 15) / 16;
+	const int grid = (int) std::min<size_t>((tiles + risltc::kMlpWarps - 1) / risltc::kMlpWarps, (size_t) ctx->sm_count * 2);
+	risltc::mlp_logits_kernel<<<grid, 32 * risltc::kMlpWarps, smem, stream>>>(q);
+	return cudaGetLastError();
+}
 
 int reserve_candidates(risltc_ctx_t* ctx, size_t need) {
 	if (need <= ctx->candidate_capacity) return RISLTC_OK;
@@ -556,6 +617,11 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		q.frame_count = frame_count;
 		q.uniform_fraction = settings->proposal_uniform_fraction;
 		q.logits = nullptr;
+		if (settings->proposal == risltc_proposal_learned) {
+			e = launch_logits(ctx, stream, scene->model, gbuffer, sc.logits);
+			if (e != cudaSuccess) return cuda_status(e);
+			q.logits = sc.logits;
+		}
 		q.out = sc.candidates;
 		const int warps = (int) ((pixels + risltc::kProposalWarps - 1) / risltc::kProposalWarps);
 		e = risltc::launch_proposal(q, stream, std::min(warps, ctx->sm_count * 16));
@@ -610,11 +676,14 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 	if (!ctx || !valid_call(scene, gbuffer, noise, frame_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	int st = validate_settings(settings);
 	if (st) return st;
-	if (settings->proposal == risltc_proposal_learned) return RISLTC_ERROR_UNSUPPORTED;
 	if (uses_proposal(settings) && scene->clusters.count == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (settings->proposal == risltc_proposal_learned && !scene->model) return RISLTC_ERROR_INVALID_ARGUMENT;
 	cudaSetDevice(ctx->device);
 	const size_t pixel_frames = (size_t) gbuffer->width * gbuffer->height * frame_count;
 	if (uses_proposal(settings) && (st = reserve_candidates(ctx, pixel_frames * settings->candidate_count)))
+		return st;
+	if (settings->proposal == risltc_proposal_learned &&
+	    (st = reserve_logits(ctx, (size_t) gbuffer->width * gbuffer->height * scene->clusters.count)))
 		return st;
 	if (uses_ris_pipeline(settings)) {
 		if ((st = reserve_records(ctx, pixel_frames))) return st;
@@ -631,8 +700,8 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		}
 		events = ctx->events[i];
 	}
-	const Scratch sc{ctx->d_records, ctx->d_candidates, ctx->d_samples, ctx->d_staged, ctx->d_rays, ctx->d_hits,
-	                 ctx->d_ray_count, ctx->d_light_rays};
+	const Scratch sc{ctx->d_records, ctx->d_candidates, ctx->d_logits, ctx->d_samples, ctx->d_staged, ctx->d_rays,
+	                 ctx->d_hits, ctx->d_ray_count, ctx->d_light_rays};
 	st = shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise->random_seed, animate, frame_count, out_rgb,
 	               accum, reservoirs, events);
 	if (st) return st;
@@ -644,17 +713,19 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	if (!ctx || (!items && item_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (item_count == 0) return RISLTC_OK;
 	// Validate everything before any work; size the scratch for all items.
-	size_t records = 0, wavefront = 0, lights = 0, queues = 0, candidates = 0;
+	size_t records = 0, wavefront = 0, lights = 0, queues = 0, candidates = 0, logits = 0;
 	for (uint32_t i = 0; i != item_count; ++i) {
 		const risltc_batch_item_t& it = items[i];
 		if (!valid_call(it.scene, &it.gbuffer, it.noise, it.frame_count) || it.scene->ctx != ctx)
 			return RISLTC_ERROR_INVALID_ARGUMENT;
 		int st = validate_settings(&it.settings);
 		if (st) return st;
-		if (it.settings.proposal == risltc_proposal_learned) return RISLTC_ERROR_UNSUPPORTED;
 		if (uses_proposal(&it.settings) && it.scene->clusters.count == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
+		if (it.settings.proposal == risltc_proposal_learned && !it.scene->model) return RISLTC_ERROR_INVALID_ARGUMENT;
 		const size_t pf = (size_t) it.gbuffer.width * it.gbuffer.height * it.frame_count;
 		if (uses_proposal(&it.settings)) candidates += pf * it.settings.candidate_count;
+		if (it.settings.proposal == risltc_proposal_learned)
+			logits += (size_t) it.gbuffer.width * it.gbuffer.height * it.scene->clusters.count;
 		if (uses_ris_pipeline(&it.settings)) records += pf;
 		if (uses_ray_queue(it.scene, &it.settings, pf)) {
 			wavefront += pf;
@@ -666,6 +737,7 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	int st;
 	if (records && (st = reserve_records(ctx, records))) return st;
 	if (candidates && (st = reserve_candidates(ctx, candidates))) return st;
+	if (logits && (st = reserve_logits(ctx, logits))) return st;
 	if (queues && (st = reserve_wavefront(ctx, wavefront, lights, queues))) return st;
 	cudaError_t e = cudaSuccess;
 	if (!ctx->batch_streams_created) {
@@ -682,7 +754,7 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	if ((e = cudaEventRecord(ctx->batch_fork, ctx->stream)) != cudaSuccess) return cuda_status(e);
 	for (int k = 0; k != streams; ++k)
 		if ((e = cudaStreamWaitEvent(ctx->batch_streams[k], ctx->batch_fork, 0)) != cudaSuccess) return cuda_status(e);
-	size_t r_off = 0, w_off = 0, l_off = 0, q_off = 0, c_off = 0;
+	size_t r_off = 0, w_off = 0, l_off = 0, q_off = 0, c_off = 0, g_off = 0;
 	for (uint32_t i = 0; i != item_count; ++i) {
 		const risltc_batch_item_t& it = items[i];
 		const size_t pf = (size_t) it.gbuffer.width * it.gbuffer.height * it.frame_count;
@@ -694,6 +766,10 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 		if (uses_proposal(&it.settings)) {
 			sc.candidates = ctx->d_candidates + c_off;
 			c_off += pf * it.settings.candidate_count;
+		}
+		if (it.settings.proposal == risltc_proposal_learned) {
+			sc.logits = ctx->d_logits + g_off;
+			g_off += (size_t) it.gbuffer.width * it.gbuffer.height * it.scene->clusters.count;
 		}
 		if (uses_ray_queue(it.scene, &it.settings, pf)) {
 			sc.samples = ctx->d_samples + w_off;
@@ -829,4 +905,122 @@ EXTERN_C const char* risltc_status_string(int status) {
 	case RISLTC_ERROR_TOO_LARGE: return "frame larger than the static scratch of risltc_shade_noalloc";
 	default: return "unknown status";
 	}
+}
+
+// ------------------------------------------------------------ learned model --
+
+EXTERN_C uint32_t risltc_model_parameter_count(uint32_t cluster_count) {
+	return (uint32_t) risltc::mlp_layout((int) cluster_count).total;
+}
+
+static int model_upload(risltc_model_t* m, const float* host) {
+	cudaSetDevice(m->ctx->device);
+	cudaError_t e = cudaMemcpy(m->d_params, host, sizeof(float) * m->parameter_count, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return cuda_status(e);
+	risltc::mlp_convert_kernel<<<64, 256, 0, m->ctx->stream>>>(m->d_params, m->d_weights, m->parameter_count);
+	e = cudaGetLastError();
+	if (e == cudaSuccess) e = cudaStreamSynchronize(m->ctx->stream);
+	return cuda_status(e);
+}
+
+EXTERN_C int risltc_model_create(risltc_ctx_t* ctx, uint32_t cluster_count, uint64_t seed, risltc_model_t** out) {
+	if (!ctx || !out || cluster_count == 0 || cluster_count > (uint32_t) risltc::kMaxClusters || cluster_count % 8)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	*out = nullptr;
+	risltc_model_t* m = (risltc_model_t*) calloc(1, sizeof(risltc_model_t));
+	if (!m) return RISLTC_ERROR_OUT_OF_MEMORY;
+	m->ctx = ctx;
+	m->cluster_count = (int) cluster_count;
+	m->parameter_count = (int) risltc_model_parameter_count(cluster_count);
+	m->inv_half_extent = 1.0f;
+	cudaSetDevice(ctx->device);
+	cudaError_t e = cudaMalloc(&m->d_params, sizeof(float) * m->parameter_count);
+	if (e == cudaSuccess) e = cudaMalloc(&m->d_weights, sizeof(__nv_bfloat16) * m->parameter_count);
+	if (e != cudaSuccess) {
+		risltc_model_destroy(m);
+		return cuda_status(e);
+	}
+	// He-uniform weights (the output layer scaled by 0.1 so that the first
+	// proposal is close to uniform), zero biases; splitmix64 for the seed.
+	std::vector<float> host(m->parameter_count, 0.0f);
+	const risltc::MlpLayout lay = risltc::mlp_layout(m->cluster_count);
+	uint64_t state = seed;
+	auto next = [&]() {
+		uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+		z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+		z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+		z ^= z >> 31;
+		return (double) (z >> 11) * (1.0 / 9007199254740992.0);
+	};
+	auto fill = [&](int offset, int count, int fan_in, double scale) {
+		const double bound = scale * std::sqrt(6.0 / fan_in);
+		for (int j = 0; j != count; ++j) host[offset + j] = (float) ((2.0 * next() - 1.0) * bound);
+	};
+	fill(lay.w1, risltc::kMlpHidden * risltc::kMlpFeatures, 130, 1.0);
+	fill(lay.w2, risltc::kMlpHidden * risltc::kMlpHidden, risltc::kMlpHidden, 1.0);
+	fill(lay.w3, m->cluster_count * risltc::kMlpHidden, risltc::kMlpHidden, 0.1);
+	// The padding features (130..143) carry no weight.
+	for (int o = 0; o != risltc::kMlpHidden; ++o)
+		for (int f = 130; f != risltc::kMlpFeatures; ++f) host[lay.w1 + o * risltc::kMlpFeatures + f] = 0.0f;
+	const int st = model_upload(m, host.data());
+	if (st) {
+		risltc_model_destroy(m);
+		return st;
+	}
+	*out = m;
+	return RISLTC_OK;
+}
+
+EXTERN_C void risltc_model_destroy(risltc_model_t* model) {
+	if (!model) return;
+	cudaSetDevice(model->ctx->device);
+	cudaStreamSynchronize(model->ctx->stream);
+	cudaFree(model->d_params);
+	cudaFree(model->d_weights);
+	free(model);
+}
+
+EXTERN_C int risltc_model_set_params(risltc_model_t* model, const float* params) {
+	if (!model || !params) return RISLTC_ERROR_INVALID_ARGUMENT;
+	return model_upload(model, params);
+}
+
+EXTERN_C int risltc_model_get_params(const risltc_model_t* model, float* params) {
+	if (!model || !params) return RISLTC_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(model->ctx->device);
+	cudaError_t e = cudaStreamSynchronize(model->ctx->stream);
+	if (e == cudaSuccess)
+		e = cudaMemcpy(params, model->d_params, sizeof(float) * model->parameter_count, cudaMemcpyDeviceToHost);
+	return cuda_status(e);
+}
+
+EXTERN_C int risltc_model_set_input_transform(risltc_model_t* model, const float center[3], float half_extent) {
+	if (!model || !center || !(half_extent > 0.0f)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	for (int a = 0; a != 3; ++a) model->center[a] = center[a];
+	model->inv_half_extent = 1.0f / half_extent;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_scene_set_model(risltc_scene_t* scene, risltc_model_t* model) {
+	if (!scene) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (model && (model->ctx != scene->ctx || model->cluster_count != scene->clusters.count))
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	scene->model = model;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_model_logits(risltc_ctx_t* ctx, const risltc_model_t* model, const risltc_gbuffer_t* gbuffer,
+                                 float* logits) {
+	if (!ctx || !model || !gbuffer || !gbuffer->planes || !logits || model->ctx != ctx || gbuffer->width == 0 ||
+	    gbuffer->height == 0)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	const size_t count = (size_t) gbuffer->width * gbuffer->height * model->cluster_count;
+	int st = reserve_logits(ctx, count);
+	if (st) return st;
+	cudaError_t e = launch_logits(ctx, ctx->stream, model, gbuffer, ctx->d_logits);
+	if (e == cudaSuccess) {
+		risltc::bf16_to_f32_kernel<<<256, 256, 0, ctx->stream>>>(ctx->d_logits, logits, count);
+		e = cudaGetLastError();
+	}
+	return cuda_status(e);
 }

@@ -18,6 +18,7 @@
 // probability written out is computed from the same cumulative values that
 // the draw compares against.
 #pragma once
+#include <cuda_bf16.h>
 #include "shade_device.cuh"
 
 namespace risltc {
@@ -47,7 +48,7 @@ struct ProposalParams {
 	int candidate_count;
 	uint32_t noise_seed, animate, frame_count;
 	float uniform_fraction;
-	const float* logits;          // [pixel][cluster], or null for cluster_weight
+	const __nv_bfloat16* logits;  // [pixel][cluster], or null for cluster_weight
 	ProposalCandidate* out;       // [frame][pixel][candidate]
 };
 
@@ -94,7 +95,7 @@ static __global__ void __launch_bounds__(32 * kProposalWarps) proposal_kernel(Pr
 		float logit_max = -INFINITY;
 		if (pr.logits)
 			for (int j = 0; j != per_lane; ++j)
-				if (k0 + j < k_count) logit_max = fmaxf(logit_max, pr.logits[(size_t) i * k_count + k0 + j]);
+				if (k0 + j < k_count) logit_max = fmaxf(logit_max, __bfloat162float(pr.logits[(size_t) i * k_count + k0 + j]));
 		if (pr.logits)
 			for (int d = 16; d != 0; d >>= 1) logit_max = fmaxf(logit_max, __shfl_xor_sync(0xffffffffu, logit_max, d));
 		for (int j = 0; j != per_lane; ++j) {
@@ -103,7 +104,7 @@ static __global__ void __launch_bounds__(32 * kProposalWarps) proposal_kernel(Pr
 			const bool empty = pr.clusters.offsets[k + 1] == pr.clusters.offsets[k];
 			float w;
 			if (pr.logits)
-				w = empty ? 0.0f : __expf(pr.logits[(size_t) i * k_count + k] - logit_max);
+				w = empty ? 0.0f : __expf(__bfloat162float(pr.logits[(size_t) i * k_count + k]) - logit_max);
 			else
 				w = empty ? 0.0f : cluster_weight(pr.clusters.bounds[k], pr.clusters.power[k], x, n);
 			local += w;

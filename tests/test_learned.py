@@ -1,0 +1,126 @@
+"""The learned cluster proposal's model (risltc_model_*): the tensor-core
+forward pass against a NumPy restatement (BF16 weights and activations, FP32
+sums), and the learned proposal's unbiasedness."""
+import numpy as np
+import pytest
+
+import golden_data as gd
+from test_proposal import clustered
+
+
+def bf16(x):
+    """Round FP32 to BF16 (nearest even), returned as FP32."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return (r & 0xFFFFFFFF).astype(np.uint32).view(np.float32)
+
+
+def encode(gbuffer, center, half_extent):
+    g = gbuffer.astype(np.float64)
+    u = np.concatenate([(g[0:3] - np.asarray(center, np.float64)[:, None]) * np.float32(1.0 / half_extent),
+                        g[3:6], g[6:9], g[16:17]], axis=0).T  # [P, 10]
+    feats = []
+    for i in range(10):
+        x = u[:, i]
+        cols = [x] + [np.sin(np.pi * x * 2.0 ** k) for k in range(6)] + [np.cos(np.pi * x * 2.0 ** k) for k in range(6)]
+        feats += cols
+    f = np.stack(feats, axis=1)
+    return np.concatenate([f, np.zeros((f.shape[0], 14))], axis=1).astype(np.float32)
+
+
+def reference_logits(params, k, features):
+    o = 0
+    def take(n):
+        nonlocal o
+        v = params[o:o + n]
+        o += n
+        return v
+    w1 = bf16(take(64 * 144)).reshape(64, 144).astype(np.float64)
+    b1 = take(64).astype(np.float64)
+    w2 = bf16(take(64 * 64)).reshape(64, 64).astype(np.float64)
+    b2 = take(64).astype(np.float64)
+    w3 = bf16(take(k * 64)).reshape(k, 64).astype(np.float64)
+    b3 = take(k).astype(np.float64)
+    h = bf16(features).astype(np.float64)
+    h = bf16(np.maximum(h @ w1.T + b1, 0.0).astype(np.float32)).astype(np.float64)
+    h = bf16(np.maximum(h @ w2.T + b2, 0.0).astype(np.float32)).astype(np.float64)
+    return bf16((h @ w3.T + b3).astype(np.float32))
+
+
+def test_parameter_count():
+    import risltc_gb300 as rl
+    lib = rl._native.load()
+    assert lib.risltc_model_parameter_count(256) == 64 * 144 + 64 + 64 * 64 + 64 + 256 * 64 + 256
+
+
+@pytest.mark.gpu
+def test_model_logits_match_numpy(gpu):
+    import torch
+    import risltc_gb300 as rl
+    sc = gd.scene("hf")
+    ctx = rl.Context(0)
+    model = rl.Model(ctx, 64, seed=7)
+    rng = np.random.default_rng(1)
+    params = model.get_params()
+    # Larger output weights and non-zero biases than the initialisation.
+    params[64 * 144 + 64 + 64 * 64 + 64:] *= 10.0
+    params[64 * 144:64 * 144 + 64] = rng.normal(0, 0.1, 64)
+    model.set_params(params)
+    center, half = (0.5, -0.25, 1.0), 6.0
+    model.set_input_transform(center, half)
+    g = torch.from_numpy(np.ascontiguousarray(sc["gbuffer"])).cuda()
+    got = model.logits(g, sc["width"], sc["height"]).cpu().numpy()
+    ctx.check()
+    model.close()
+    ctx.close()
+    want = reference_logits(params, 64, encode(sc["gbuffer"], center, half))
+    err = np.abs(got - want)
+    scale = np.abs(want).max()
+    assert np.quantile(err, 0.999) <= 0.02 * scale
+    assert err.max() <= 0.08 * scale
+    print("logits: scale %.3f, median error %.2e, max error %.2e" % (scale, np.median(err), err.max()))
+
+
+@pytest.mark.gpu
+def test_learned_proposal_is_unbiased(gpu):
+    import torch
+    import risltc_gb300 as rl
+    from test_unbiased import BATCHES, FRAMES_PER_BATCH
+    sc, offsets, _, _ = clustered(gd.scene("hf"), 8)
+    ctx = rl.Context(0)
+    l0, l1, k = gd.ltc()
+    scene = rl.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    scene.set_clusters(offsets)
+    model = rl.Model(ctx, 8, seed=3)
+    params = model.get_params()
+    params[64 * 144 + 64 + 64 * 64 + 64:] *= 20.0  # a strongly non-uniform proposal
+    model.set_params(params)
+    model.set_input_transform((0.0, 0.0, 1.0), 6.0)
+    scene.set_model(model)
+    p = sc["width"] * sc["height"]
+    g = torch.from_numpy(np.ascontiguousarray(sc["gbuffer"])).cuda()
+    out = torch.zeros((p, 3), dtype=torch.float32, device="cuda")
+
+    def means(settings, seed0):
+        m = np.zeros((BATCHES, p, 3))
+        for b in range(BATCHES):
+            rl.shade(ctx, scene, g, sc["width"], sc["height"], settings, noise_seed=seed0 + b * FRAMES_PER_BATCH,
+                     frames=FRAMES_PER_BATCH, out_rgb=out)
+            m[b] = out.cpu().numpy()
+        return m
+
+    a = means(rl.settings(candidates=32, proposal="learned", proposal_uniform_fraction=0.1), 0)
+    b = means(rl.settings(technique="projected_solid_angle", light_sampling="uniform"), 1_000_000)
+    ctx.check()
+    scene.close()
+    model.close()
+    ctx.close()
+    ma, mb = a.mean(0), b.mean(0)
+    se = np.sqrt(a.var(0, ddof=1) / BATCHES + b.var(0, ddof=1) / BATCHES)
+    lit = se > 1e-6 * np.maximum(np.abs(mb), 1e-30)
+    z = (ma - mb)[lit] / se[lit]
+    print("learned proposal: %d pixel-channels, z mean %.3f, variance %.3f, max |z| %.2f"
+          % (z.size, z.mean(), z.var(), np.abs(z).max()))
+    assert abs(z.mean()) < 0.15
+    assert 0.7 < z.var() < 1.4
+    assert (np.abs(z) > 5.0).mean() < 0.002
