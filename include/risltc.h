@@ -346,6 +346,14 @@ EXTERN_C int risltc_model_create(risltc_ctx_t* ctx, uint32_t cluster_count, uint
 EXTERN_C void risltc_model_destroy(risltc_model_t* model);
 EXTERN_C int risltc_model_set_params(risltc_model_t* model, const float* params);
 EXTERN_C int risltc_model_get_params(const risltc_model_t* model, float* params);
+/* Online training: while enabled, every risltc_shade call that uses this
+   model for the learned proposal also trains it on its own RIS candidates
+   (frame 0, every pixel_stride-th pixel, the phase following the noise
+   seed): the candidates' weights p_hat / p give each cluster's share of the
+   pixel's shading, the loss is its cross entropy with softmax(logits), and
+   one Adam step (beta 0.9 / 0.999) with the given learning rate follows the
+   call's kernels.  Defaults: off, 1e-3, 64. */
+EXTERN_C int risltc_model_set_training(risltc_model_t* model, int enable, float learning_rate, uint32_t pixel_stride);
 /* Inputs: position (p - center) / half_extent. */
 EXTERN_C int risltc_model_set_input_transform(risltc_model_t* model, const float center[3], float half_extent);
 /* The model the scene's learned proposal uses (its cluster count must match

@@ -108,3 +108,31 @@ void oracle_f32_proposal(const oracle_scene_t* s, const oracle_settings_t* st, c
 		pdfs[c] = out[c].pdf;
 	}
 }
+
+/* The LTC-CP target p_hat = length(evaluate_polygonal_light_shading) of every
+   light at pixel i of the G-buffer (shading_pass.frag.glsl:421-456, 732). */
+void oracle_f32_ltc_cp_targets(const oracle_scene_t* s, const oracle_settings_t* st, const oracle_gbuffer_t* gbuffer,
+                               uint32_t i, float* p_hat) {
+	ctx_t c;
+	c.scene = s;
+	c.settings = st;
+	c.maxv = (uint32_t) s->max_light_vertex_count;
+	c.maxp = c.maxv + 1;
+	const size_t np = (size_t) gbuffer->width * gbuffer->height;
+	const float* g = gbuffer->planes;
+	shading_data_t sd;
+	sd.position = V3(g[0 * np + i], g[1 * np + i], g[2 * np + i]);
+	sd.normal = V3(g[3 * np + i], g[4 * np + i], g[5 * np + i]);
+	sd.outgoing = V3(g[6 * np + i], g[7 * np + i], g[8 * np + i]);
+	sd.lambert_outgoing = g[9 * np + i];
+	sd.diffuse_albedo = V3(g[10 * np + i], g[11 * np + i], g[12 * np + i]);
+	sd.fresnel_0 = V3(g[13 * np + i], g[14 * np + i], g[15 * np + i]);
+	sd.roughness = g[16 * np + i];
+	float fl = v3_dot(sd.fresnel_0, V3(0.2126f, 0.7152f, 0.0722f));
+	ltc_coefficients_t ltc = get_ltc_coefficients(s, fl, sd.roughness, sd.position, sd.normal, sd.outgoing);
+	for (int l = 0; l != s->light_count; ++l) {
+		light_t light;
+		load_light(s, l, &light);
+		p_hat[l] = v3_length(ltc_cp_target(&c, &sd, ltc, &light));
+	}
+}

@@ -186,6 +186,10 @@ class Model:
         check(self._lib.risltc_model_set_params(self._h, p.ctypes.data_as(_native.c_float_p)),
               "risltc_model_set_params")
 
+    def set_training(self, enable=True, learning_rate=1e-3, pixel_stride=64):
+        check(self._lib.risltc_model_set_training(self._h, int(enable), learning_rate, pixel_stride),
+              "risltc_model_set_training")
+
     def set_input_transform(self, center, half_extent):
         c = np.ascontiguousarray(center, np.float32)
         check(self._lib.risltc_model_set_input_transform(self._h, c.ctypes.data_as(_native.c_float_p),

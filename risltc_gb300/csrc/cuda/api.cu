@@ -90,6 +90,14 @@ struct risltc_model_s {
 	float* d_params;             // FP32 parameters (risltc_model_parameter_count)
 	__nv_bfloat16* d_weights;    // their BF16 copy used by the kernels
 	float center[3], inv_half_extent;
+	// Online training (risltc_model_set_training): gradient, Adam moments.
+	float* d_grad;
+	float* d_adam_m;
+	float* d_adam_v;
+	int training;
+	float learning_rate;
+	uint32_t pixel_stride;
+	uint32_t steps;
 };
 
 namespace {
@@ -515,6 +523,55 @@ int reserve_logits(risltc_ctx_t* ctx, size_t need) {
 	return RISLTC_OK;
 }
 
+// One training step of the scene's model on frame 0's candidates of the
+// training pixels, then an Adam update (stream-ordered).
+cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_scene_t* scene,
+                            const risltc_gbuffer_t* gbuffer, const risltc::ProposalCandidate* candidates,
+                            int candidate_count, uint32_t stride, uint32_t phase) {
+	risltc_model_t* m = scene->model;
+	const uint32_t np = gbuffer->width * gbuffer->height;
+	const uint32_t n_train = np > phase ? (np - phase + stride - 1) / stride : 0;
+	if (n_train == 0) return cudaSuccess;
+	risltc::MlpTrainParams t;
+	memset(&t, 0, sizeof(t));
+	t.gbuffer = gbuffer->planes;
+	t.width = gbuffer->width;
+	t.height = gbuffer->height;
+	t.params = m->d_params;
+	t.grad = m->d_grad;
+	t.k_count = m->cluster_count;
+	for (int a = 0; a != 3; ++a) t.center[a] = m->center[a];
+	t.inv_half_extent = m->inv_half_extent;
+	t.offsets = scene->clusters.offsets;
+	t.light_cluster = scene->clusters.light_cluster;
+	t.primitive = gbuffer->primitive;
+	t.candidates = candidates;
+	t.candidate_count = candidate_count;
+	t.stride = stride;
+	t.phase = phase;
+	t.inv_batch = 1.0f / (float) n_train;
+	static std::atomic<uint64_t> configured{0};
+	const uint64_t bit = 1ull << (ctx->device & 63);
+	if (!(configured.load() & bit)) {
+		cudaError_t e = cudaFuncSetAttribute(risltc::mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                     (int) risltc::mlp_train_smem_bytes(risltc::kMaxClusters));
+		if (e != cudaSuccess) return e;
+		configured.fetch_or(bit);
+	}
+	const int blocks = (int) std::min<uint32_t>((n_train + risltc::kTrainPixels - 1) / risltc::kTrainPixels,
+	                                            (uint32_t) ctx->sm_count);
+	risltc::mlp_train_kernel<<<blocks, risltc::kTrainThreads, risltc::mlp_train_smem_bytes(m->cluster_count), stream>>>(t);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	m->steps += 1;
+	const double b1 = 0.9, b2 = 0.999;
+	risltc::mlp_adam_kernel<<<64, 256, 0, stream>>>(m->d_params, m->d_grad, m->d_adam_m, m->d_adam_v, m->d_weights,
+	                                               m->parameter_count, m->learning_rate, (float) b1, (float) b2, 1e-8f,
+	                                               (float) (1.0 - std::pow(b1, (double) m->steps)),
+	                                               (float) (1.0 - std::pow(b2, (double) m->steps)));
+	return cudaGetLastError();
+}
+
 // The model's logits for every pixel of the G-buffer into logits.
 cudaError_t launch_logits(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_model_t* m,
                           const risltc_gbuffer_t* gbuffer, __nv_bfloat16* logits) {
@@ -648,6 +705,13 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		r.frame_count = p.frame_count;
 		r.records = sc.records;
 		r.candidates = uses_proposal(settings) ? sc.candidates : nullptr;
+		const risltc_model_t* model = scene->model;
+		const bool train = settings->proposal == risltc_proposal_learned && model && model->training;
+		if (train) {
+			r.train_candidates = sc.candidates;
+			r.train_stride = model->pixel_stride;
+			r.train_phase = noise_seed % model->pixel_stride;
+		}
 		if (uses_ray_queue(scene, settings, pixels * frame_count)) {
 			r.samples = sc.samples;
 			r.staged = sc.staged;
@@ -662,6 +726,8 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		r.error = ctx->d_error;
 		e = risltc::launch_ris(r, stream, grid_for(ctx, pixels), grid_for(ctx, 2 * pixels * frame_count), events,
 		                       fast);
+		if (e == cudaSuccess && train) e = launch_training(ctx, stream, scene, gbuffer, sc.candidates, r.candidate_count,
+		                                                    r.train_stride, r.train_phase);
 	} else {
 		e = risltc::launch_shade(p, stream, grid_for(ctx, pixels), events, fast);
 	}
@@ -936,6 +1002,12 @@ EXTERN_C int risltc_model_create(risltc_ctx_t* ctx, uint32_t cluster_count, uint
 	cudaSetDevice(ctx->device);
 	cudaError_t e = cudaMalloc(&m->d_params, sizeof(float) * m->parameter_count);
 	if (e == cudaSuccess) e = cudaMalloc(&m->d_weights, sizeof(__nv_bfloat16) * m->parameter_count);
+	for (float** buf : {&m->d_grad, &m->d_adam_m, &m->d_adam_v}) {
+		if (e == cudaSuccess) e = cudaMalloc(buf, sizeof(float) * m->parameter_count);
+		if (e == cudaSuccess) e = cudaMemset(*buf, 0, sizeof(float) * m->parameter_count);
+	}
+	m->learning_rate = 1e-3f;
+	m->pixel_stride = 64;
 	if (e != cudaSuccess) {
 		risltc_model_destroy(m);
 		return cuda_status(e);
@@ -977,6 +1049,9 @@ EXTERN_C void risltc_model_destroy(risltc_model_t* model) {
 	cudaStreamSynchronize(model->ctx->stream);
 	cudaFree(model->d_params);
 	cudaFree(model->d_weights);
+	cudaFree(model->d_grad);
+	cudaFree(model->d_adam_m);
+	cudaFree(model->d_adam_v);
 	free(model);
 }
 
@@ -1023,4 +1098,12 @@ EXTERN_C int risltc_model_logits(risltc_ctx_t* ctx, const risltc_model_t* model,
 		e = cudaGetLastError();
 	}
 	return cuda_status(e);
+}
+
+EXTERN_C int risltc_model_set_training(risltc_model_t* model, int enable, float learning_rate, uint32_t pixel_stride) {
+	if (!model || !(learning_rate > 0.0f) || pixel_stride == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
+	model->training = enable != 0;
+	model->learning_rate = learning_rate;
+	model->pixel_stride = pixel_stride;
+	return RISLTC_OK;
 }

@@ -14,6 +14,7 @@
 // BF16, so the hidden activations never leave the registers.
 #pragma once
 #include <cuda_bf16.h>
+#include "proposal.cuh"
 #include "shade_device.cuh"
 
 namespace risltc {
@@ -219,6 +220,189 @@ static __global__ void mlp_convert_kernel(const float* params, __nv_bfloat16* we
 static __global__ void bf16_to_f32_kernel(const __nv_bfloat16* in, float* out, size_t count) {
 	for (size_t j = blockIdx.x * (size_t) blockDim.x + threadIdx.x; j < count; j += (size_t) gridDim.x * blockDim.x)
 		out[j] = __bfloat162float(in[j]);
+}
+
+}  // namespace risltc
+
+namespace risltc {
+
+// ----------------------------------------------------------------- training --
+// Online training of the proposal on the RIS candidates of a frame: for each
+// training pixel the candidates' weights w = p_hat / p (the LTC-CP target
+// over the proposal probability, written back by the candidate kernel) give
+// an estimate of each cluster's share of the pixel's shading, F_c; the loss
+// is the cross entropy between the normalised estimate T_c = F_c / sum F and
+// q = softmax(logits), whose gradient in the logits is (q - T) / B over the
+// B training pixels.  Forward and backward run in FP32 from the FP32 master
+// parameters, one block per 32 training pixels, partial weight gradients
+// summed in shared memory and added to the gradient vector once per block.
+constexpr int kTrainPixels = 32;   // training pixels per block step
+constexpr int kTrainThreads = 256;
+
+struct MlpTrainParams {
+	const float* gbuffer;
+	uint32_t width, height;
+	const float* params;          // FP32 parameter vector
+	float* grad;                  // FP32 gradient vector (accumulated)
+	int k_count;
+	float center[3], inv_half_extent;
+	const uint32_t* offsets;      // cluster offsets (light -> cluster via light_cluster)
+	const uint32_t* light_cluster;
+	const uint32_t* primitive;
+	// Frame 0's candidates [pixel][candidate] after the candidate kernel wrote
+	// each training pixel's RIS weights w = p_hat / p into their pdf field.
+	const ProposalCandidate* candidates;
+	int candidate_count;
+	uint32_t stride, phase;       // training pixels: i % stride == phase
+	float inv_batch;              // 1 / number of training pixels
+};
+
+inline size_t mlp_train_smem_bytes(int k_count) {
+	return sizeof(float) * kTrainPixels * (kMlpFeatures + 4 * kMlpHidden + k_count);
+}
+
+static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrainParams pr) {
+	extern __shared__ __align__(16) float train_smem[];
+	const int k_count = pr.k_count;
+	const MlpLayout lay = mlp_layout(k_count);
+	float* feat = train_smem;                          // [32][144]
+	float* h1 = feat + kTrainPixels * kMlpFeatures;    // [32][64]
+	float* h2 = h1 + kTrainPixels * kMlpHidden;        // [32][64]
+	float* dz = h2 + kTrainPixels * kMlpHidden;        // [32][K] logits, then their gradient
+	float* d2 = dz + kTrainPixels * k_count;           // [32][64]
+	float* d1 = d2 + kTrainPixels * kMlpHidden;        // [32][64]
+	const uint32_t np = pr.width * pr.height;
+	const uint32_t n_train = np > pr.phase ? (np - pr.phase + pr.stride - 1) / pr.stride : 0;
+	const int tid = threadIdx.x;
+	for (uint32_t base = blockIdx.x * kTrainPixels; base < n_train; base += gridDim.x * kTrainPixels) {
+		// Encode the block's training pixels (invalid ones get zero weight).
+		for (int idx = tid; idx < kTrainPixels * kMlpFeatures; idx += kTrainThreads) {
+			const int r = idx / kMlpFeatures, f = idx % kMlpFeatures;
+			const uint32_t j = base + r, i = pr.phase + j * pr.stride;
+			float v = 0.0f;
+			if (j < n_train) {
+				float u[kMlpInputs];
+				mlp_inputs(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, u);
+				v = mlp_feature(u, f);
+			}
+			feat[idx] = v;
+		}
+		__syncthreads();
+		// Forward: h1, h2 (ReLU), logits.
+		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
+			const int r = idx / kMlpHidden, o = idx % kMlpHidden;
+			float acc = pr.params[lay.b1 + o];
+			const float* w = pr.params + lay.w1 + o * kMlpFeatures;
+			for (int f = 0; f != kMlpFeatures; ++f) acc += w[f] * feat[r * kMlpFeatures + f];
+			h1[idx] = fmaxf(acc, 0.0f);
+		}
+		__syncthreads();
+		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
+			const int r = idx / kMlpHidden, o = idx % kMlpHidden;
+			float acc = pr.params[lay.b2 + o];
+			const float* w = pr.params + lay.w2 + o * kMlpHidden;
+			for (int f = 0; f != kMlpHidden; ++f) acc += w[f] * h1[r * kMlpHidden + f];
+			h2[idx] = fmaxf(acc, 0.0f);
+		}
+		__syncthreads();
+		for (int idx = tid; idx < kTrainPixels * k_count; idx += kTrainThreads) {
+			const int r = idx / k_count, o = idx % k_count;
+			float acc = pr.params[lay.b3 + o];
+			const float* w = pr.params + lay.w3 + o * kMlpHidden;
+			for (int f = 0; f != kMlpHidden; ++f) acc += w[f] * h2[r * kMlpHidden + f];
+			dz[idx] = acc;
+		}
+		__syncthreads();
+		// Softmax and target per pixel: one warp per pixel.
+		for (int r = tid / 32; r < kTrainPixels; r += kTrainThreads / 32) {
+			const int lane = tid % 32;
+			const uint32_t j = base + r, i = pr.phase + j * pr.stride;
+			const bool valid = j < n_train && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
+			float* z = dz + r * k_count;
+			float m = -INFINITY;
+			for (int c = lane; c < k_count; c += 32) m = fmaxf(m, z[c]);
+			for (int d = 16; d != 0; d >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, d));
+			float sum = 0.0f;
+			for (int c = lane; c < k_count; c += 32) {
+				const float e = __expf(z[c] - m);
+				z[c] = e;
+				sum += e;
+			}
+			for (int d = 16; d != 0; d >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, d);
+			// Target: the candidates' weights summed per cluster.
+			float total = 0.0f;
+			if (valid)
+				for (int c = lane; c < pr.candidate_count; c += 32) total += pr.candidates[(size_t) i * pr.candidate_count + c].pdf;
+			for (int d = 16; d != 0; d >>= 1) total += __shfl_xor_sync(0xffffffffu, total, d);
+			__syncwarp();
+			const bool learn = valid && total > 0.0f && total <= 3.0e38f;
+			const float inv_sum = 1.0f / sum;
+			for (int c = lane; c < k_count; c += 32) z[c] = learn ? z[c] * inv_sum * pr.inv_batch : 0.0f;
+			__syncwarp();
+			if (learn)
+				for (int c = lane; c < pr.candidate_count; c += 32) {
+					const ProposalCandidate q = pr.candidates[(size_t) i * pr.candidate_count + c];
+					if (q.pdf > 0.0f) atomicAdd(&z[pr.light_cluster[q.light]], -q.pdf / total * pr.inv_batch);
+				}
+			__syncwarp();
+		}
+		__syncthreads();
+		// Backward: d2 = (W3^T dz) * [h2 > 0], d1 = (W2^T d2) * [h1 > 0].
+		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
+			const int r = idx / kMlpHidden, f = idx % kMlpHidden;
+			float acc = 0.0f;
+			for (int o = 0; o != k_count; ++o) acc += pr.params[lay.w3 + o * kMlpHidden + f] * dz[r * k_count + o];
+			d2[idx] = h2[idx] > 0.0f ? acc : 0.0f;
+		}
+		__syncthreads();
+		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
+			const int r = idx / kMlpHidden, f = idx % kMlpHidden;
+			float acc = 0.0f;
+			for (int o = 0; o != kMlpHidden; ++o) acc += pr.params[lay.w2 + o * kMlpHidden + f] * d2[r * kMlpHidden + o];
+			d1[idx] = h1[idx] > 0.0f ? acc : 0.0f;
+		}
+		__syncthreads();
+		// Weight gradients summed over the block's pixels, added once.
+		for (int idx = tid; idx < k_count * (kMlpHidden + 1); idx += kTrainThreads) {
+			const int o = idx / (kMlpHidden + 1), f = idx % (kMlpHidden + 1);
+			float acc = 0.0f;
+			for (int r = 0; r != kTrainPixels; ++r) acc += dz[r * k_count + o] * (f < kMlpHidden ? h2[r * kMlpHidden + f] : 1.0f);
+			if (acc != 0.0f) atomicAdd(pr.grad + (f < kMlpHidden ? lay.w3 + o * kMlpHidden + f : lay.b3 + o), acc);
+		}
+		for (int idx = tid; idx < kMlpHidden * (kMlpHidden + 1); idx += kTrainThreads) {
+			const int o = idx / (kMlpHidden + 1), f = idx % (kMlpHidden + 1);
+			float acc = 0.0f;
+			for (int r = 0; r != kTrainPixels; ++r) acc += d2[r * kMlpHidden + o] * (f < kMlpHidden ? h1[r * kMlpHidden + f] : 1.0f);
+			if (acc != 0.0f) atomicAdd(pr.grad + (f < kMlpHidden ? lay.w2 + o * kMlpHidden + f : lay.b2 + o), acc);
+		}
+		for (int idx = tid; idx < kMlpHidden * (kMlpFeatures + 1); idx += kTrainThreads) {
+			const int o = idx / (kMlpFeatures + 1), f = idx % (kMlpFeatures + 1);
+			float acc = 0.0f;
+			for (int r = 0; r != kTrainPixels; ++r) acc += d1[r * kMlpHidden + o] * (f < kMlpFeatures ? feat[r * kMlpFeatures + f] : 1.0f);
+			if (acc != 0.0f) atomicAdd(pr.grad + (f < kMlpFeatures ? lay.w1 + o * kMlpFeatures + f : lay.b1 + o), acc);
+		}
+		__syncthreads();
+	}
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 parameters; clears the gradient and
+// refreshes the BF16 copy.  The padding features' weights stay zero.
+static __global__ void mlp_adam_kernel(float* params, float* grad, float* m, float* v, __nv_bfloat16* weights, int count,
+                                       float learning_rate, float beta1, float beta2, float epsilon, float correction1,
+                                       float correction2) {
+	for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+		const float g = grad[j];
+		const float mj = beta1 * m[j] + (1.0f - beta1) * g;
+		const float vj = beta2 * v[j] + (1.0f - beta2) * g * g;
+		m[j] = mj;
+		v[j] = vj;
+		const bool padding = j < kMlpHidden * kMlpFeatures && j % kMlpFeatures >= kMlpInputs * 13;
+		float p = params[j];
+		if (!padding) p -= learning_rate * (mj / correction1) / (sqrtf(vj / correction2) + epsilon);
+		params[j] = p;
+		weights[j] = __float2bfloat16_rn(p);
+		grad[j] = 0.0f;
+	}
 }
 
 }  // namespace risltc

@@ -350,6 +350,8 @@ ris_candidates_binned_kernel(RisParams pr) {
 						const float rnd = get_noise_1(seed);
 						const float p_hat = tile.p_hat[lane * kSuper + k];
 						const float w = P::div(p_hat, pk);
+						if (pr.train_stride && f == 0 && i % pr.train_stride == pr.train_phase)
+							pr.train_candidates[(size_t) i * pr.candidate_count + cs + k].pdf = w;
 						w_sum += w;
 						if (w > 0.0f && rnd < P::div(w, w_sum)) {
 							res_index = idx;

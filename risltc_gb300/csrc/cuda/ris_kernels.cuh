@@ -42,6 +42,11 @@ struct RisParams {
 	// Candidates drawn by a proposal ([frame][pixel][candidate]); null: each
 	// candidate is drawn uniformly from the pixel's noise as in the reference.
 	const ProposalCandidate* candidates;
+	// With train_stride != 0, frame 0's candidates of the pixels with
+	// i % train_stride == train_phase get their RIS weight p_hat / pdf written
+	// over the pdf (the training data of the learned proposal).
+	ProposalCandidate* train_candidates;
+	uint32_t train_stride, train_phase;
 	// Shadow rays traced in their own pass (null: traced in ris_shade_kernel).
 	struct SampleRecord* samples;  // [frame][pixel]
 	struct ShadowRay* staged;      // [frame][pixel][technique], as generated

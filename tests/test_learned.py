@@ -124,3 +124,72 @@ def test_learned_proposal_is_unbiased(gpu):
     assert abs(z.mean()) < 0.15
     assert 0.7 < z.var() < 1.4
     assert (np.abs(z) > 5.0).mean() < 0.002
+
+
+def exact_cluster_targets(sc, offsets):
+    """Per pixel, each cluster's share of the LTC-CP targets of all lights
+    (the distribution the learned proposal is trained towards)."""
+    import ctypes
+    import oracle as orc
+    from test_proposal import oracle_scene
+    from risltc_gb300 import scenes
+    bounds, power = scenes.cluster_summaries(sc["lights"], sc["max_vertex_count"], offsets)
+    osc = oracle_scene(sc, offsets, bounds, power)
+    lib = orc.load()
+    lib.oracle_f32_ltc_cp_targets.argtypes = [ctypes.POINTER(orc.Scene), ctypes.POINTER(orc.Settings),
+                                              ctypes.POINTER(orc.GBuffer), ctypes.c_uint32, ctypes.c_void_p]
+    st = orc.make_settings()
+    g = orc.GBuffer()
+    g.width, g.height = sc["width"], sc["height"]
+    planes = np.ascontiguousarray(sc["gbuffer"], np.float32)
+    g.planes = planes.ctypes.data
+    n = sc["lights"].shape[0]
+    k = offsets.size - 1
+    cluster = np.repeat(np.arange(k), np.diff(offsets.astype(np.int64)))
+    out = np.zeros((g.width * g.height, k))
+    p_hat = np.zeros(n, np.float32)
+    for i in range(g.width * g.height):
+        lib.oracle_f32_ltc_cp_targets(ctypes.byref(osc.struct), ctypes.byref(st), ctypes.byref(g), i,
+                                      p_hat.ctypes.data)
+        out[i] = np.bincount(cluster, weights=p_hat.astype(np.float64), minlength=k)
+    return out
+
+
+def mean_kl(targets, logits):
+    t = targets / np.maximum(targets.sum(1, keepdims=True), 1e-30)
+    z = logits - logits.max(1, keepdims=True)
+    logq = z - np.log(np.exp(z).sum(1, keepdims=True))
+    keep = targets.sum(1) > 0
+    kl = (t * (np.log(np.maximum(t, 1e-30)) - logq)).sum(1)
+    return float(kl[keep].mean())
+
+
+@pytest.mark.gpu
+def test_online_training_moves_the_proposal_towards_the_targets(gpu):
+    import torch
+    import risltc_gb300 as rl
+    sc, offsets, _, _ = clustered(gd.scene("hf"), 8)
+    targets = exact_cluster_targets(sc, offsets)
+    ctx = rl.Context(0)
+    l0, l1, k = gd.ltc()
+    scene = rl.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    scene.set_clusters(offsets)
+    model = rl.Model(ctx, 8, seed=5)
+    model.set_input_transform((0.0, 0.0, 1.0), 6.0)
+    scene.set_model(model)
+    g = torch.from_numpy(np.ascontiguousarray(sc["gbuffer"])).cuda()
+    p = sc["width"] * sc["height"]
+    out = torch.zeros((p, 3), dtype=torch.float32, device="cuda")
+    before = mean_kl(targets, model.logits(g, sc["width"], sc["height"]).cpu().numpy())
+    model.set_training(True, learning_rate=3e-3, pixel_stride=1)
+    s = rl.settings(candidates=32, proposal="learned", proposal_uniform_fraction=0.1)
+    for call in range(300):
+        rl.shade(ctx, scene, g, sc["width"], sc["height"], s, noise_seed=call, frames=1, out_rgb=out)
+    ctx.check()
+    after = mean_kl(targets, model.logits(g, sc["width"], sc["height"]).cpu().numpy())
+    assert np.isfinite(model.get_params()).all()
+    print("KL(target || proposal): %.4f before training, %.4f after 300 steps" % (before, after))
+    scene.close()
+    model.close()
+    ctx.close()
+    assert after < 0.5 * before
