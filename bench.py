@@ -50,6 +50,11 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--workload", choices=["throughput", "equal-mse"], default="throughput",
+                   help="equal-mse: device time to equal MSE, learned cluster proposal vs plain RIS")
+    p.add_argument("--clusters", type=int, default=256)
+    p.add_argument("--train-frames", type=int, default=64)
+    p.add_argument("--reference-spp", type=int, default=4096)
     return p.parse_args()
 
 
@@ -378,11 +383,114 @@ def run_ours(a, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def run_equal_mse(a):
+    """Device time to equal MSE, learned cluster proposal vs plain RIS.
+
+    Heightfield frame with a.lights lights k-means-grouped into a.clusters
+    clusters and a.triangles occluders.  Reference: a.reference_spp spp of
+    plain RIS accumulated in FP64 on the GPU.  The learned proposal's model
+    trains online for a.train_frames frames first (1 spp each, every 16th
+    pixel); then each method renders a.spp spp four times with fresh noise
+    and its MSE against the reference is measured, with its device time per
+    frame (CUDA events, training off).  MSE falls as 1 / spp for these
+    unbiased estimators, so the time to reach plain RIS's a.spp-spp MSE is
+    ms_per_frame * spp * MSE(method) / MSE(plain)."""
+    import torch
+    import risltc_gb300 as rl
+    from risltc_gb300 import scenes
+    hs0 = make_workload(a, seed=0)
+    hs, offsets = scenes.cluster_lights(hs0, a.clusters, seed=1)
+    ctx = rl.Context(0)
+    scene = rl.Scene.from_host_scene(ctx, hs)
+    scene.set_clusters(offsets)
+    model = rl.Model(ctx, a.clusters, seed=2)
+    model.set_input_transform((0.0, 0.0, 1.0), 6.0)
+    scene.set_model(model)
+    P = hs.pixels
+    covered = torch.from_numpy(hs.primitive == 0).cuda() if hs.primitive is not None else None
+    g = torch.from_numpy(hs.gbuffer).cuda()
+    prim = torch.from_numpy(hs.primitive.view(np.int32)).cuda()
+    plain = rl.settings(candidates=a.candidates)
+    clusters = rl.settings(candidates=a.candidates, proposal="clusters", proposal_uniform_fraction=0.1)
+    learned = rl.settings(candidates=a.candidates, proposal="learned", proposal_uniform_fraction=0.1)
+    # Reference: FP64 running sums of plain RIS.
+    acc = torch.zeros((P, 3), dtype=torch.float64, device="cuda")
+    seed = 10_000_000
+    for _ in range(a.reference_spp // 16):
+        seed = rl.shade(ctx, scene, g, hs.width, hs.height, plain, noise_seed=seed, frames=16, accum=acc,
+                        primitive=prim)
+    reference = acc / (16 * (a.reference_spp // 16))
+    ctx.check()
+    # Online training of the model (1 spp per call, its own candidates).
+    model.set_training(True, learning_rate=2e-3, pixel_stride=16)
+    out = torch.empty((P, 3), dtype=torch.float32, device="cuda")
+    seed = 20_000_000
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(a.train_frames):
+        seed = rl.shade(ctx, scene, g, hs.width, hs.height, learned, noise_seed=seed, frames=1, out_rgb=out,
+                        primitive=prim)
+    t1.record()
+    torch.cuda.synchronize()
+    train_ms = t0.elapsed_time(t1) / max(a.train_frames, 1)
+    model.set_training(False)
+    results = {}
+    for name, s in (("plain", plain), ("clusters", clusters), ("learned", learned)):
+        mses = []
+        for rep in range(4):
+            rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=30_000_000 + 1000 * rep, frames=a.spp,
+                     out_rgb=out, primitive=prim)
+            d = (out.double() - reference) ** 2
+            if covered is not None:
+                d = d[covered]
+            mses.append(float(d.mean()))
+        for _ in range(a.warmup):
+            rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=4, out_rgb=out, primitive=prim)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(a.steps):
+            rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=40_000_000 + 4 * i, frames=4, out_rgb=out,
+                     primitive=prim)
+        e1.record()
+        torch.cuda.synchronize()
+        results[name] = {"mse_at_spp": statistics.mean(mses), "ms_per_frame": e0.elapsed_time(e1) / (4 * a.steps)}
+    ctx.check()
+    base = results["plain"]
+    for r in results.values():
+        r["ms_to_plain_mse"] = r["ms_per_frame"] * a.spp * r["mse_at_spp"] / base["mse_at_spp"]
+    line = {
+        "metric": "ms/frame to equal MSE, learned-proposal vs plain RIS (%dx%d, %d lights); Gsamples/s"
+                  % (hs.width, hs.height, hs.light_count),
+        "value": results["learned"]["ms_to_plain_mse"], "unit": "ms", "higher_is_better": False,
+        "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "dtype": "f32 (MLP bf16/fp32)", "data": "synthetic",
+        "config": {"workload": "equal MSE: %dx%d fBm heightfield, %d polygon lights (3-8 vertices) in %d k-means "
+                               "clusters, %dk occluder triangles, M=%d, MSE at %d spp against a %d-spp FP64 plain-RIS "
+                               "reference" % (hs.width, hs.height, hs.light_count, a.clusters, a.triangles // 1000,
+                                              a.candidates, a.spp, a.reference_spp),
+                   "train_frames": a.train_frames, "train_ms_per_frame": train_ms},
+        "plain_ms_to_equal_mse": base["ms_to_plain_mse"],
+        "speedup_vs_plain": base["ms_to_plain_mse"] / results["learned"]["ms_to_plain_mse"],
+        "methods": results,
+        "gsamples_per_s": {k: hs.pixels / (v["ms_per_frame"] / 1e3) / 1e9 for k, v in results.items()},
+    }
+    print(json.dumps(line), flush=True)
+    scene.close()
+    model.close()
+    ctx.close()
+
+
 def main():
     a = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.workload == "equal-mse":
+        if rank == 0 and a.impl == "ours":
+            run_equal_mse(a)
+        return
     if a.impl == "reference":
         run_reference(a, rank, world)
     else:
