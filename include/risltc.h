@@ -354,6 +354,12 @@ EXTERN_C int risltc_model_get_params(const risltc_model_t* model, float* params)
    one Adam step (beta 0.9 / 0.999) with the given learning rate follows the
    call's kernels.  Defaults: off, 1e-3, 64. */
 EXTERN_C int risltc_model_set_training(risltc_model_t* model, int enable, float learning_rate, uint32_t pixel_stride);
+/* The training target's mix (default 0.5): with weight 1 - shadowed_weight
+   the candidates' unshadowed per-cluster shares, with shadowed_weight the
+   frame's final shaded estimate (with shadow rays) attributed to the chosen
+   light's cluster, which makes the proposal learn visibility.  The shadowed
+   part needs shadows on and one sample per technique. */
+EXTERN_C int risltc_model_set_target_mix(risltc_model_t* model, float shadowed_weight);
 /* Inputs: position (p - center) / half_extent. */
 EXTERN_C int risltc_model_set_input_transform(risltc_model_t* model, const float center[3], float half_extent);
 /* The model the scene's learned proposal uses (its cluster count must match

@@ -122,6 +122,7 @@ SIGNATURES = {
     "risltc_model_get_params": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     "risltc_model_set_input_transform": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_float]),
     "risltc_model_set_training": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_uint32]),
+    "risltc_model_set_target_mix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float]),
     "risltc_scene_set_model": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "risltc_model_logits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer), ctypes.c_void_p]),
     "risltc_default_settings": (None, [ctypes.POINTER(Settings)]),

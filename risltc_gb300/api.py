@@ -190,6 +190,9 @@ class Model:
         check(self._lib.risltc_model_set_training(self._h, int(enable), learning_rate, pixel_stride),
               "risltc_model_set_training")
 
+    def set_target_mix(self, shadowed_weight):
+        check(self._lib.risltc_model_set_target_mix(self._h, float(shadowed_weight)), "risltc_model_set_target_mix")
+
     def set_input_transform(self, center, half_extent):
         c = np.ascontiguousarray(center, np.float32)
         check(self._lib.risltc_model_set_input_transform(self._h, c.ctypes.data_as(_native.c_float_p),

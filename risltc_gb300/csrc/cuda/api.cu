@@ -98,6 +98,9 @@ struct risltc_model_s {
 	float learning_rate;
 	uint32_t pixel_stride;
 	uint32_t steps;
+	float shadowed_weight;
+	float* d_shaded;             // frame 0's shaded luminance of the training pixels
+	size_t shaded_capacity;
 };
 
 namespace {
@@ -527,7 +530,8 @@ int reserve_logits(risltc_ctx_t* ctx, size_t need) {
 // training pixels, then an Adam update (stream-ordered).
 cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_scene_t* scene,
                             const risltc_gbuffer_t* gbuffer, const risltc::ProposalCandidate* candidates,
-                            int candidate_count, uint32_t stride, uint32_t phase) {
+                            int candidate_count, uint32_t stride, uint32_t phase, const float* shaded,
+                            const risltc::ReservoirRecord* records) {
 	risltc_model_t* m = scene->model;
 	const uint32_t np = gbuffer->width * gbuffer->height;
 	const uint32_t n_train = np > phase ? (np - phase + stride - 1) / stride : 0;
@@ -550,6 +554,9 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 	t.stride = stride;
 	t.phase = phase;
 	t.inv_batch = 1.0f / (float) n_train;
+	t.shaded = shaded;
+	t.records = reinterpret_cast<const int4*>(records);
+	t.shadowed_weight = m->shadowed_weight;
 	static std::atomic<uint64_t> configured{0};
 	const uint64_t bit = 1ull << (ctx->device & 63);
 	if (!(configured.load() & bit)) {
@@ -711,6 +718,17 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 			r.train_candidates = sc.candidates;
 			r.train_stride = model->pixel_stride;
 			r.train_phase = noise_seed % model->pixel_stride;
+			if (model->shadowed_weight > 0.0f && uses_ray_queue(scene, settings, pixels * frame_count)) {
+				risltc_model_t* mm = scene->model;
+				if (mm->shaded_capacity < pixels) {
+					cudaFree(mm->d_shaded);
+					mm->d_shaded = nullptr;
+					mm->shaded_capacity = 0;
+					if ((e = cudaMalloc(&mm->d_shaded, pixels * sizeof(float))) != cudaSuccess) return cuda_status(e);
+					mm->shaded_capacity = pixels;
+				}
+				r.train_shaded = mm->d_shaded;
+			}
 		}
 		if (uses_ray_queue(scene, settings, pixels * frame_count)) {
 			r.samples = sc.samples;
@@ -726,8 +744,9 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		r.error = ctx->d_error;
 		e = risltc::launch_ris(r, stream, grid_for(ctx, pixels), grid_for(ctx, 2 * pixels * frame_count), events,
 		                       fast);
-		if (e == cudaSuccess && train) e = launch_training(ctx, stream, scene, gbuffer, sc.candidates, r.candidate_count,
-		                                                    r.train_stride, r.train_phase);
+		if (e == cudaSuccess && train)
+			e = launch_training(ctx, stream, scene, gbuffer, sc.candidates, r.candidate_count, r.train_stride,
+			                    r.train_phase, r.train_shaded, r.records);
 	} else {
 		e = risltc::launch_shade(p, stream, grid_for(ctx, pixels), events, fast);
 	}
@@ -1008,6 +1027,7 @@ EXTERN_C int risltc_model_create(risltc_ctx_t* ctx, uint32_t cluster_count, uint
 	}
 	m->learning_rate = 1e-3f;
 	m->pixel_stride = 64;
+	m->shadowed_weight = 0.5f;
 	if (e != cudaSuccess) {
 		risltc_model_destroy(m);
 		return cuda_status(e);
@@ -1052,6 +1072,7 @@ EXTERN_C void risltc_model_destroy(risltc_model_t* model) {
 	cudaFree(model->d_grad);
 	cudaFree(model->d_adam_m);
 	cudaFree(model->d_adam_v);
+	cudaFree(model->d_shaded);
 	free(model);
 }
 
@@ -1105,5 +1126,11 @@ EXTERN_C int risltc_model_set_training(risltc_model_t* model, int enable, float 
 	model->training = enable != 0;
 	model->learning_rate = learning_rate;
 	model->pixel_stride = pixel_stride;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_model_set_target_mix(risltc_model_t* model, float shadowed_weight) {
+	if (!model || !(shadowed_weight >= 0.0f && shadowed_weight <= 1.0f)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	model->shadowed_weight = shadowed_weight;
 	return RISLTC_OK;
 }

@@ -230,10 +230,15 @@ namespace risltc {
 // Online training of the proposal on the RIS candidates of a frame: for each
 // training pixel the candidates' weights w = p_hat / p (the LTC-CP target
 // over the proposal probability, written back by the candidate kernel) give
-// an estimate of each cluster's share of the pixel's shading, F_c; the loss
-// is the cross entropy between the normalised estimate T_c = F_c / sum F and
-// q = softmax(logits), whose gradient in the logits is (q - T) / B over the
-// B training pixels.  Forward and backward run in FP32 from the FP32 master
+// an estimate of each cluster's share of the pixel's unshadowed shading,
+// F_c; the loss is the cross entropy between the normalised estimate
+// T_c = F_c / sum F and q = softmax(logits), whose gradient in the logits is
+// (q - T) / B over the B training pixels.  The shadowed part: the frame's
+// final estimate f(y) W for the chosen light y is an unbiased estimate of the
+// shadowed shading of y's cluster alone (RIS integrates f times the cluster's
+// indicator), so with s = lum(f W) over the unshadowed estimate sum w / M
+// (clamped to 4) it adds s (q - onehot(cluster(y))) / B; the two parts are
+// mixed by shadowed_weight.  Forward and backward run in FP32 from the FP32 master
 // parameters, one block per 32 training pixels, partial weight gradients
 // summed in shared memory and added to the gradient vector once per block.
 constexpr int kTrainPixels = 32;   // training pixels per block step
@@ -255,6 +260,13 @@ struct MlpTrainParams {
 	int candidate_count;
 	uint32_t stride, phase;       // training pixels: i % stride == phase
 	float inv_batch;              // 1 / number of training pixels
+	// The shadowed part of the target (may be null): the frame's shaded
+	// luminance per training pixel and its reservoir records (the chosen
+	// light in .x), weighted by shadowed_weight against the unshadowed
+	// candidate target.
+	const float* shaded;
+	const int4* records;
+	float shadowed_weight;
 };
 
 inline size_t mlp_train_smem_bytes(int k_count) {
@@ -337,13 +349,23 @@ static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrai
 			__syncwarp();
 			const bool learn = valid && total > 0.0f && total <= 3.0e38f;
 			const float inv_sum = 1.0f / sum;
-			for (int c = lane; c < k_count; c += 32) z[c] = learn ? z[c] * inv_sum * pr.inv_batch : 0.0f;
+			const float wu = pr.shaded ? 1.0f - pr.shadowed_weight : 1.0f;
+			float ss = 0.0f;
+			int chosen = -1;
+			if (learn && pr.shaded) {
+				chosen = pr.records[i].x;
+				ss = chosen >= 0 ? pr.shaded[i] / (total / (float) pr.candidate_count) : 0.0f;
+				ss = pr.shadowed_weight * fminf(fmaxf(ss, 0.0f), 4.0f);
+			}
+			for (int c = lane; c < k_count; c += 32) z[c] = learn ? (wu + ss) * z[c] * inv_sum * pr.inv_batch : 0.0f;
 			__syncwarp();
-			if (learn)
+			if (learn) {
 				for (int c = lane; c < pr.candidate_count; c += 32) {
 					const ProposalCandidate q = pr.candidates[(size_t) i * pr.candidate_count + c];
-					if (q.pdf > 0.0f) atomicAdd(&z[pr.light_cluster[q.light]], -q.pdf / total * pr.inv_batch);
+					if (q.pdf > 0.0f) atomicAdd(&z[pr.light_cluster[q.light]], -wu * q.pdf / total * pr.inv_batch);
 				}
+				if (lane == 0 && chosen >= 0 && ss > 0.0f) atomicAdd(&z[pr.light_cluster[chosen]], -ss * pr.inv_batch);
+			}
 			__syncwarp();
 		}
 		__syncthreads();

@@ -47,6 +47,9 @@ struct RisParams {
 	// over the pdf (the training data of the learned proposal).
 	ProposalCandidate* train_candidates;
 	uint32_t train_stride, train_phase;
+	// Frame 0's shaded luminance (with visibility) of those pixels, from the
+	// resolve kernel (may be null).
+	float* train_shaded;
 	// Shadow rays traced in their own pass (null: traced in ris_shade_kernel).
 	struct SampleRecord* samples;  // [frame][pixel]
 	struct ShadowRay* staged;      // [frame][pixel][technique], as generated

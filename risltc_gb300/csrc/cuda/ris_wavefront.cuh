@@ -355,9 +355,12 @@ template <class P> __global__ void __launch_bounds__(128) ris_resolve_kernel(Ris
 				const f3 cw = scale(color, q3.x);
 				final_color = add(final_color, mk3(P::div(cw.x, 1.0f), P::div(cw.y, 1.0f), P::div(cw.z, 1.0f)));
 			}
-			if (isnan(final_color.x) || isnan(final_color.y) || isnan(final_color.z) || isinf(final_color.x) ||
-			    isinf(final_color.y) || isinf(final_color.z))
-				final_color = mk3(1.0f, 0.0f, 0.8f);
+			const bool finite = !(isnan(final_color.x) || isnan(final_color.y) || isnan(final_color.z) ||
+			                      isinf(final_color.x) || isinf(final_color.y) || isinf(final_color.z));
+			if (f == 0 && pr.train_shaded && pr.train_stride && i % pr.train_stride == pr.train_phase)
+				pr.train_shaded[i] =
+				    finite ? 0.2126f * final_color.x + 0.7152f * final_color.y + 0.0722f * final_color.z : 0.0f;
+			if (!finite) final_color = mk3(1.0f, 0.0f, 0.8f);
 			if (f == 0 && res) {
 				const ReservoirRecord r = pr.records[pf];
 				*res = risltc_reservoir_t{r.light_index, r.w_sum, r.p_hat, 0u};

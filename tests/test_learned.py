@@ -182,6 +182,7 @@ def test_online_training_moves_the_proposal_towards_the_targets(gpu):
     out = torch.zeros((p, 3), dtype=torch.float32, device="cuda")
     before = mean_kl(targets, model.logits(g, sc["width"], sc["height"]).cpu().numpy())
     model.set_training(True, learning_rate=3e-3, pixel_stride=1)
+    model.set_target_mix(0.0)  # the unshadowed targets only, as computed above
     s = rl.settings(candidates=32, proposal="learned", proposal_uniform_fraction=0.1)
     for call in range(300):
         rl.shade(ctx, scene, g, sc["width"], sc["height"], s, noise_seed=call, frames=1, out_rgb=out)
