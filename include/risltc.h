@@ -370,6 +370,31 @@ EXTERN_C int risltc_scene_set_model(risltc_scene_t* scene, risltc_model_t* model
 EXTERN_C int risltc_model_logits(risltc_ctx_t* ctx, const risltc_model_t* model, const risltc_gbuffer_t* gbuffer,
                                  float* logits);
 
+/* A G-buffer producer for the synthetic heightfield scenes (the role of the
+   reference's visibility pass and get_shading_data,
+   shading_pass.frag.glsl:571-672, which rasterise meshes): a pinhole camera
+   at `camera` looking at the origin (z up, vertical field of view fov_y in
+   radians) sees the surface z = sum_w amplitude sin(fx x + fy y + phase);
+   per pixel the first crossing (10 steps across the height band, then 12
+   bisections), the gradient normal adapted into the view hemisphere, and a
+   material hashed from (pixel, material_seed): roughness and per-channel
+   albedo uniform in their ranges, F0 = fresnel_0.  planes: 17 x width x
+   height floats and primitive: width x height (0 hit, 0xFFFFFFFF miss),
+   device memory, stream-ordered. */
+#define RISLTC_MAX_WAVES 16
+typedef struct risltc_heightfield_s {
+	float camera[3];
+	float fov_y;
+	uint32_t wave_count;
+	float waves[RISLTC_MAX_WAVES][4];
+	uint32_t material_seed;
+	float roughness_min, roughness_max;
+	float albedo_min, albedo_max;
+	float fresnel_0;
+} risltc_heightfield_t;
+EXTERN_C int risltc_gbuffer_heightfield(risltc_ctx_t* ctx, const risltc_heightfield_t* heightfield, uint32_t width,
+                                        uint32_t height, float* planes, uint32_t* primitive);
+
 /* Uploads lights (the std140 buffer of risltc_write_lights), the LTC table
    and, if triangle_count > 0, builds and uploads the BVH of the occluders
    (9 floats per triangle; fewer than 2^28 triangles, else

@@ -75,6 +75,14 @@ class Camera(ctypes.Structure):
                 ("rotation_x_0", ctypes.c_float), ("rotation_z_0", ctypes.c_float)]
 
 
+class Heightfield(ctypes.Structure):
+    """risltc_heightfield_t."""
+    _fields_ = [("camera", ctypes.c_float * 3), ("fov_y", ctypes.c_float), ("wave_count", ctypes.c_uint32),
+                ("waves", (ctypes.c_float * 4) * 16), ("material_seed", ctypes.c_uint32),
+                ("roughness_min", ctypes.c_float), ("roughness_max", ctypes.c_float),
+                ("albedo_min", ctypes.c_float), ("albedo_max", ctypes.c_float), ("fresnel_0", ctypes.c_float)]
+
+
 class BatchItem(ctypes.Structure):
     """risltc_batch_item_t."""
     _fields_ = [("scene", ctypes.c_void_p), ("gbuffer", GBuffer), ("settings", Settings),
@@ -125,6 +133,8 @@ SIGNATURES = {
     "risltc_model_set_target_mix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float]),
     "risltc_scene_set_model": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "risltc_model_logits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer), ctypes.c_void_p]),
+    "risltc_gbuffer_heightfield": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Heightfield), ctypes.c_uint32,
+                                                  ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]),
     "risltc_default_settings": (None, [ctypes.POINTER(Settings)]),
     "risltc_ctx_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]),
     "risltc_ctx_destroy": (None, [ctypes.c_void_p]),

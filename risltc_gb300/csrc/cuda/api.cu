@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 #include <cuda_runtime.h>
+#include "gbuffer.cuh"
 #include "mlp.cuh"
 #include "ris_wavefront.cuh"
 
@@ -1133,4 +1134,54 @@ EXTERN_C int risltc_model_set_target_mix(risltc_model_t* model, float shadowed_w
 	if (!model || !(shadowed_weight >= 0.0f && shadowed_weight <= 1.0f)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	model->shadowed_weight = shadowed_weight;
 	return RISLTC_OK;
+}
+
+// ------------------------------------------------------------- G-buffers --
+
+EXTERN_C int risltc_gbuffer_heightfield(risltc_ctx_t* ctx, const risltc_heightfield_t* hf, uint32_t width,
+                                        uint32_t height, float* planes, uint32_t* primitive) {
+	if (!ctx || !hf || !planes || width == 0 || height == 0 || hf->wave_count > RISLTC_MAX_WAVES ||
+	    !(hf->fov_y > 0.0f && hf->fov_y < 3.1f) || (uint64_t) width * height > 0xffffffffull / 32)
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	risltc::HeightfieldParams p;
+	memset(&p, 0, sizeof(p));
+	// Camera basis in double: forward towards the origin, right, up.
+	const double c[3] = {hf->camera[0], hf->camera[1], hf->camera[2]};
+	const double len = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+	if (!(len > 0.0)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	const double f[3] = {-c[0] / len, -c[1] / len, -c[2] / len};
+	double r[3] = {f[1], -f[0], 0.0};  // cross(f, z)
+	const double rl = std::sqrt(r[0] * r[0] + r[1] * r[1]);
+	if (!(rl > 0.0)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	for (double& x : r) x /= rl;
+	const double u[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+	for (int a = 0; a != 3; ++a) {
+		p.camera[a] = hf->camera[a];
+		p.forward[a] = (float) f[a];
+		p.right[a] = (float) r[a];
+		p.up[a] = (float) u[a];
+	}
+	const double th = std::tan(0.5 * hf->fov_y);
+	p.tan_half_y = (float) th;
+	p.tan_half_x = (float) (th * width / height);
+	p.wave_count = (int) hf->wave_count;
+	double hmax = 0.0;
+	for (uint32_t w = 0; w != hf->wave_count; ++w) {
+		for (int k = 0; k != 4; ++k) p.waves[w][k] = hf->waves[w][k];
+		hmax += std::fabs(hf->waves[w][0]);
+	}
+	p.max_height = (float) hmax;
+	p.material_seed = hf->material_seed;
+	p.roughness_min = hf->roughness_min;
+	p.roughness_max = hf->roughness_max;
+	p.albedo_min = hf->albedo_min;
+	p.albedo_max = hf->albedo_max;
+	p.fresnel_0 = hf->fresnel_0;
+	p.width = width;
+	p.height = height;
+	p.planes = planes;
+	p.primitive = primitive;
+	cudaSetDevice(ctx->device);
+	risltc::heightfield_gbuffer_kernel<<<grid_for(ctx, (size_t) width * height), 128, 0, ctx->stream>>>(p);
+	return cuda_status(cudaGetLastError());
 }

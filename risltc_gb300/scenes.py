@@ -320,6 +320,36 @@ def _height_grad(waves, x, y):
     return gx, gy
 
 
+def heightfield_gbuffer_gpu(ctx, width, height, seed=0, camera=(0.0, -9.0, 6.0), fov_y_degrees=60.0,
+                            material_seed=None):
+    """risltc_gbuffer_heightfield: the heightfield() surface (same waves for
+    the same seed) shaded into a G-buffer on the GPU.  Returns (planes
+    [17, H*W], primitive [H*W] int32) as torch device tensors.  Materials come
+    from a per-pixel hash, not from NumPy's generator."""
+    import torch
+    rng = np.random.default_rng(seed)
+    waves = _heightfield_waves(rng)
+    hf = _native.Heightfield()
+    for a in range(3):
+        hf.camera[a] = camera[a]
+    hf.fov_y = float(np.radians(fov_y_degrees))
+    hf.wave_count = waves.shape[0]
+    for w in range(waves.shape[0]):
+        for k in range(4):
+            hf.waves[w][k] = float(waves[w, k])
+    hf.material_seed = seed if material_seed is None else material_seed
+    hf.roughness_min, hf.roughness_max = 0.05, 1.0
+    hf.albedo_min, hf.albedo_max = 0.2, 0.8
+    hf.fresnel_0 = F0_DIELECTRIC
+    planes = torch.empty((GBUFFER_PLANES, width * height), dtype=torch.float32, device="cuda")
+    prim = torch.empty(width * height, dtype=torch.int32, device="cuda")
+    _native.check(_native.load().risltc_gbuffer_heightfield(ctx.handle, ctypes.byref(hf), width, height,
+                                                            ctypes.c_void_p(planes.data_ptr()),
+                                                            ctypes.c_void_p(prim.data_ptr())),
+                  "risltc_gbuffer_heightfield")
+    return planes, prim
+
+
 def heightfield(width=1920, height=1080, light_count=1024, triangle_count=200_000, seed=0, vertex_counts=(3, 8),
                 ltc_size=64, light_lib=None, camera=(0.0, -9.0, 6.0), fov_y_degrees=60.0):
     """Configuration 2: fBm heightfield G-buffer, polygon lights, occluders."""
