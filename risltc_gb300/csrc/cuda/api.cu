@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include "gbuffer.cuh"
 #include "mlp.cuh"
+#include "ris_binned.cuh"
 #include "ris_wavefront.cuh"
 
 namespace risltc {
@@ -32,6 +33,12 @@ struct risltc_ctx_s {
 	// Reservoir records between the candidate and shading kernels.
 	risltc::ReservoirRecord* d_records;
 	size_t record_capacity;
+	// The binned candidate kernel's per-warp p_hat slots: one region per
+	// stream that may run it at the same time (the context's stream and the
+	// batch streams share regions 0..RISLTC_BATCH_STREAMS-1), each with a slot
+	// per warp of the largest grid (sm_count * 16 blocks of 4 warps).
+	float* d_phat;
+	int phat_regions;
 	// Proposal candidates (light, pdf) per pixel-frame and candidate.
 	risltc::ProposalCandidate* d_candidates;
 	size_t candidate_capacity;
@@ -265,6 +272,7 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	cudaFree(ctx->d_rgb);
 	cudaFreeHost(ctx->h_pinned_rgb);
 	cudaFree(ctx->d_records);
+	cudaFree(ctx->d_phat);
 	cudaFree(ctx->d_candidates);
 	cudaFree(ctx->d_logits);
 	cudaFree(ctx->d_samples);
@@ -502,6 +510,7 @@ bool uses_ray_queue(const risltc_scene_t* scene, const risltc_settings_t* s, siz
 // One call's share of the context's scratch.
 struct Scratch {
 	risltc::ReservoirRecord* records;
+	float* p_hat;
 	risltc::ProposalCandidate* candidates;
 	__nv_bfloat16* logits;
 	risltc::SampleRecord* samples;
@@ -623,6 +632,23 @@ int reserve_candidates(risltc_ctx_t* ctx, size_t need) {
 	return RISLTC_OK;
 }
 
+size_t phat_region_floats(const risltc_ctx_t* ctx) {
+	return (size_t) ctx->sm_count * 16 * risltc::kBinnedWarps * risltc::kPHatSlot;
+}
+
+int reserve_phat(risltc_ctx_t* ctx, int regions) {
+	if (regions <= ctx->phat_regions) return RISLTC_OK;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(ctx->d_phat);
+	ctx->d_phat = nullptr;
+	ctx->phat_regions = 0;
+	cudaError_t e = cudaMalloc(&ctx->d_phat, sizeof(float) * phat_region_floats(ctx) * regions);
+	if (e != cudaSuccess) return cuda_status(e);
+	ctx->phat_regions = regions;
+	return RISLTC_OK;
+}
+
 int reserve_records(risltc_ctx_t* ctx, size_t need) {
 	if (need <= ctx->record_capacity) return RISLTC_OK;
 	cudaSetDevice(ctx->device);
@@ -712,6 +738,7 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		r.animate = p.animate;
 		r.frame_count = p.frame_count;
 		r.records = sc.records;
+		r.p_hat_scratch = sc.p_hat;
 		r.candidates = uses_proposal(settings) ? sc.candidates : nullptr;
 		const risltc_model_t* model = scene->model;
 		const bool train = settings->proposal == risltc_proposal_learned && model && model->training;
@@ -773,6 +800,7 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		return st;
 	if (uses_ris_pipeline(settings)) {
 		if ((st = reserve_records(ctx, pixel_frames))) return st;
+		if ((st = reserve_phat(ctx, 1))) return st;
 		if (uses_ray_queue(scene, settings, pixel_frames) &&
 		    (st = reserve_wavefront(ctx, pixel_frames, scene->view.light_count)))
 			return st;
@@ -786,8 +814,8 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		}
 		events = ctx->events[i];
 	}
-	const Scratch sc{ctx->d_records, ctx->d_candidates, ctx->d_logits, ctx->d_samples, ctx->d_staged, ctx->d_rays,
-	                 ctx->d_hits, ctx->d_ray_count, ctx->d_light_rays};
+	const Scratch sc{ctx->d_records, ctx->d_phat, ctx->d_candidates, ctx->d_logits, ctx->d_samples, ctx->d_staged,
+	                 ctx->d_rays, ctx->d_hits, ctx->d_ray_count, ctx->d_light_rays};
 	st = shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise->random_seed, animate, frame_count, out_rgb,
 	               accum, reservoirs, events);
 	if (st) return st;
@@ -822,6 +850,7 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	cudaSetDevice(ctx->device);
 	int st;
 	if (records && (st = reserve_records(ctx, records))) return st;
+	if (records && (st = reserve_phat(ctx, RISLTC_BATCH_STREAMS))) return st;
 	if (candidates && (st = reserve_candidates(ctx, candidates))) return st;
 	if (logits && (st = reserve_logits(ctx, logits))) return st;
 	if (queues && (st = reserve_wavefront(ctx, wavefront, lights, queues))) return st;
@@ -847,6 +876,7 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 		Scratch sc{};
 		if (uses_ris_pipeline(&it.settings)) {
 			sc.records = ctx->d_records + r_off;
+			sc.p_hat = ctx->d_phat + phat_region_floats(ctx) * (i % RISLTC_BATCH_STREAMS);
 			r_off += pf;
 		}
 		if (uses_proposal(&it.settings)) {

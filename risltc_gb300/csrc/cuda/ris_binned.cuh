@@ -26,9 +26,6 @@
 
 namespace risltc {
 
-#ifndef RISLTC_CANDIDATES_BINNED
-#define RISLTC_CANDIDATES_BINNED 1
-#endif
 #ifndef RISLTC_BINNED_CHUNK
 #define RISLTC_BINNED_CHUNK 8
 #endif
@@ -37,6 +34,11 @@ namespace risltc {
 #endif
 constexpr int kChunk = RISLTC_BINNED_CHUNK;  // candidates per pixel per chunk
 constexpr int kItems = 32 * kChunk;          // items per warp per chunk
+// A warp's p_hat values of one super-chunk, [pixel lane][candidate], live in
+// its slot of RisParams::p_hat_scratch (global memory, L2/L1): keeping them
+// out of shared memory leaves room in the SM's combined L1/shared storage
+// for the light records the candidates read.
+constexpr int kPHatSlot = 32 * 32;
 constexpr int kDeferred = kItems + 32;       // deferred items pending at most
 
 // Candidates per pixel per super-chunk (measured best: 32 in exact numerics,
@@ -60,7 +62,6 @@ template <int kSuper> struct WarpTile {
 	float frame[32][kFrameWords];
 	int32_t item_light[kItems];
 	uint16_t item_slot[kItems];  // pixel lane * kSuper + candidate of the super-chunk
-	float p_hat[32 * kSuper];    // [pixel lane][candidate of the super-chunk]
 	int32_t deferred_light[kDeferred];
 	uint16_t deferred_slot[kDeferred];
 	uint32_t deferred_count;
@@ -192,7 +193,9 @@ __global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
 ris_candidates_binned_kernel(RisParams pr) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	constexpr int kSuper = BinnedSuper<P>::value;
+	static_assert(32 * kSuper <= kPHatSlot, "p_hat slot");
 	WarpTile<kSuper>& tile = reinterpret_cast<WarpTile<kSuper>*>(smem_raw)[threadIdx.x / 32];
+	float* const phat = pr.p_hat_scratch + (size_t) (blockIdx.x * kBinnedWarps + threadIdx.x / 32) * kPHatSlot;
 	const uint32_t lane = threadIdx.x % 32;
 	const uint32_t np = pr.width * pr.height;
 	const int n_lights = pr.scene.light_count;
@@ -302,7 +305,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 							const int32_t l = tile.item_light[it];
 							float ph;
 							if (binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph)) {
-								tile.p_hat[slot] = ph;
+								phat[slot] = ph;
 							} else {
 								const uint32_t d = atomicAdd(&tile.deferred_count, 1u);
 								tile.deferred_light[d] = l;
@@ -317,7 +320,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 						float ph = 0.0f;
 						binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, tile.deferred_light[d]),
 						                    true, ph);
-						tile.p_hat[slot] = ph;
+						phat[slot] = ph;
 						__syncwarp();
 						if (lane == 0) tile.deferred_count = pending - 32;
 						__syncwarp();
@@ -330,7 +333,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 					float ph = 0.0f;
 					binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, tile.deferred_light[lane]),
 					                    true, ph);
-					tile.p_hat[slot] = ph;
+					phat[slot] = ph;
 				}
 				__syncwarp();
 				// 4. Reservoir updates in candidate order, drawing the same
@@ -348,7 +351,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 							pk = q.pdf;
 						}
 						const float rnd = get_noise_1(seed);
-						const float p_hat = tile.p_hat[lane * kSuper + k];
+						const float p_hat = phat[lane * kSuper + k];
 						const float w = P::div(p_hat, pk);
 						if (pr.train_stride && f == 0 && i % pr.train_stride == pr.train_phase)
 							pr.train_candidates[(size_t) i * pr.candidate_count + cs + k].pdf = w;
@@ -379,6 +382,12 @@ template <class P> constexpr size_t binned_smem_bytes() {
 // kernel runs on a device (once, so that later launches, including those
 // captured into a CUDA graph, make no other runtime call).
 template <class P> cudaError_t launch_candidates_binned(const RisParams& p, cudaStream_t stream, int grid) {
+	// Without p_hat scratch (the allocation-free entry point), the kernel with
+	// one thread per pixel computes the same records.
+	if (!p.p_hat_scratch) {
+		ris_candidates_kernel<P><<<grid, 128, 0, stream>>>(p);
+		return cudaGetLastError();
+	}
 	static std::atomic<uint64_t> configured{0};
 	int device = 0;
 	cudaError_t e = cudaGetDevice(&device);

@@ -39,6 +39,10 @@ struct RisParams {
 	uint32_t animate;
 	uint32_t frame_count;
 	ReservoirRecord* records;  // [frame][pixel] scratch
+	// Per-warp scratch of the binned candidate kernel (one slot of 32 x 32
+	// floats per warp of the grid); null selects the one-thread-per-pixel
+	// candidate kernel.
+	float* p_hat_scratch;
 	// Candidates drawn by a proposal ([frame][pixel][candidate]); null: each
 	// candidate is drawn uniformly from the pixel's noise as in the reference.
 	const ProposalCandidate* candidates;

@@ -18,12 +18,7 @@ cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cu
 	return e;
 }
 cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid) {
-#if RISLTC_CANDIDATES_BINNED
 	return launch_candidates_binned<ExactNumerics>(p, stream, grid);
-#else
-	ris_candidates_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
-#endif
-	return cudaGetLastError();
 }
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid) {
 	ris_shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);

@@ -5,11 +5,6 @@
 
 namespace risltc {
 cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid) {
-#if RISLTC_CANDIDATES_BINNED
 	return launch_candidates_binned<FastNumerics>(p, stream, grid);
-#else
-	ris_candidates_kernel<FastNumerics><<<grid, 128, 0, stream>>>(p);
-#endif
-	return cudaGetLastError();
 }
 }  // namespace risltc
