@@ -397,7 +397,7 @@ EXTERN_C int risltc_gbuffer_heightfield(risltc_ctx_t* ctx, const risltc_heightfi
 
 /* Uploads lights (the std140 buffer of risltc_write_lights), the LTC table
    and, if triangle_count > 0, builds and uploads the BVH of the occluders
-   (9 floats per triangle; fewer than 2^28 triangles, else
+   (9 floats per triangle; fewer than 2^28 triangles and 2^22 lights, else
    RISLTC_ERROR_TOO_LARGE; all finite, else RISLTC_ERROR_NON_FINITE).  All
    inputs are host memory. */
 EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, uint32_t light_count,

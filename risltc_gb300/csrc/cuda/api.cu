@@ -298,8 +298,9 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	    max_vertex_count < 3 || max_vertex_count > RISLTC_MAX_LIGHT_VERTEX_COUNT || (triangle_count && !triangles))
 		return RISLTC_ERROR_INVALID_ARGUMENT;
 	*out = nullptr;
-	// Leaf references hold the first triangle in 28 bits.
-	if (triangle_count >= (1u << 28)) return RISLTC_ERROR_TOO_LARGE;
+	// Leaf references hold the first triangle in 28 bits; the candidate
+	// kernel's items hold a light in 22 bits.
+	if (triangle_count >= (1u << 28) || light_count >= (1u << 22)) return RISLTC_ERROR_TOO_LARGE;
 	// Finite occluders keep the traversal's box tests free of NaN.
 	for (size_t i = 0; i != 9 * (size_t) triangle_count; ++i)
 		if (!std::isfinite(triangles[i])) return RISLTC_ERROR_NON_FINITE;

@@ -60,10 +60,10 @@ static_assert(kItems < 1024, "10-bit bin counters");
 template <int kSuper> struct WarpTile {
 	static_assert(kSuper % kChunk == 0 && 32 * kSuper <= 65536, "super-chunk layout");
 	float frame[32][kFrameWords];
-	int32_t item_light[kItems];
-	uint16_t item_slot[kItems];  // pixel lane * kSuper + candidate of the super-chunk
-	int32_t deferred_light[kDeferred];
-	uint16_t deferred_slot[kDeferred];
+	// Items as light << 10 | slot, slot = pixel lane * kSuper + candidate of
+	// the super-chunk (below 1024; lights below 2^22).
+	uint32_t item[kItems];
+	uint32_t deferred[kDeferred];
 	uint32_t deferred_count;
 };
 
@@ -290,8 +290,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 								if (q == (int) b) s = start[q];
 							const uint32_t pos = s + (uint32_t) ((prefix >> (10 * b)) & 1023u);
 							prefix += 1ull << (10 * b);
-							tile.item_light[pos] = light[k];
-							tile.item_slot[pos] = (uint16_t) (lane * kSuper + c0 + k);
+							tile.item[pos] = ((uint32_t) light[k] << 10) | (lane * kSuper + c0 + k);
 						}
 					}
 					__syncwarp();
@@ -301,24 +300,24 @@ ris_candidates_binned_kernel(RisParams pr) {
 					for (uint32_t base = 0; base < item_count; base += 32) {
 						const uint32_t it = base + lane;
 						if (it < item_count) {
-							const uint32_t slot = tile.item_slot[it];
-							const int32_t l = tile.item_light[it];
+							const uint32_t item = tile.item[it];
+							const uint32_t slot = item & 1023u;
+							const int32_t l = (int32_t) (item >> 10);
 							float ph;
 							if (binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph)) {
 								phat[slot] = ph;
 							} else {
 								const uint32_t d = atomicAdd(&tile.deferred_count, 1u);
-								tile.deferred_light[d] = l;
-								tile.deferred_slot[d] = (uint16_t) slot;
+								tile.deferred[d] = item;
 							}
 						}
 					}
 					__syncwarp();
 					for (uint32_t pending = tile.deferred_count; pending >= 32; pending -= 32) {
 						const uint32_t d = pending - 32 + lane;
-						const uint32_t slot = tile.deferred_slot[d];
+						const uint32_t slot = tile.deferred[d] & 1023u;
 						float ph = 0.0f;
-						binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, tile.deferred_light[d]),
+						binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[d] >> 10)),
 						                    true, ph);
 						phat[slot] = ph;
 						__syncwarp();
@@ -329,9 +328,9 @@ ris_candidates_binned_kernel(RisParams pr) {
 				// The rest of the deferred items.
 				const uint32_t rest = tile.deferred_count;
 				if (lane < rest) {
-					const uint32_t slot = tile.deferred_slot[lane];
+					const uint32_t slot = tile.deferred[lane] & 1023u;
 					float ph = 0.0f;
-					binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, tile.deferred_light[lane]),
+					binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[lane] >> 10)),
 					                    true, ph);
 					phat[slot] = ph;
 				}
