@@ -273,10 +273,10 @@ static __global__ void __launch_bounds__(128) shadow_scatter_kernel(RisParams pr
 #define RISLTC_TRACE_REFILL 8
 #endif
 // Persistent any-hit tracing of the queue (queue[0] rays; queue[1] is the
-// fetch cursor, zero at launch).  Each lane holds one ray and advances it one
-// inner node per iteration; whenever RISLTC_TRACE_REFILL or more lanes of a
-// warp are idle they fetch the next rays together, so lanes do not wait for
-// the warp's longest ray.
+// fetch cursor, zero at launch).  Each lane holds one ray and advances it by
+// one unit of work (a triangle test or an inner node) per iteration;
+// whenever RISLTC_TRACE_REFILL or more lanes of a warp are idle they fetch
+// the next rays together, so lanes do not wait for the warp's longest ray.
 template <class P>
 __global__ void __launch_bounds__(128) shadow_trace_kernel(SceneView s, const ShadowRay* rays, uint32_t* queue,
                                                            uint8_t* hits, uint32_t* error) {

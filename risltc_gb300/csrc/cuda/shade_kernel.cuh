@@ -135,30 +135,39 @@ template <class P> RL_DEV int trace_begin(const SceneView& s, TraceRay& r, f3 o,
 	return kTraceContinue;
 }
 
-// One step.  Gives up after kTraversalLimit steps or on a stack overflow,
-// records the error and reports "not occluded".
-template <class P> RL_DEV int trace_step(const SceneView& s, TraceRay& r, int32_t* stack, uint32_t* error) {
-	if (++r.visits > kTraversalLimit) {
-		atomicOr(error, kErrorTraversalLimit);
-		return kTraceMiss;
-	}
-	if (r.leaf_left != 0) {
-		const bool hit = ray_triangle<P>(r, s.triangles + 3 * (size_t) r.leaf_first);
-		++r.leaf_first;
-		--r.leaf_left;
-		return hit ? kTraceHit : kTraceContinue;
-	}
-	if (r.node == kNoNode) {
-		if (r.sp == 0) return kTraceMiss;
-		r.node = stack[--r.sp];
-	}
-	if (r.node < 0) {
+// The ray's next unit of work: kWorkTriangle (the current leaf's next
+// triangle) or kWorkNode (an inner node), resolving the current reference or
+// the top of the stack and opening leaves on the way; kWorkDone when nothing
+// is left.  Calling it again before the work is done returns the same unit.
+enum : int { kWorkTriangle = 0, kWorkNode = 1, kWorkDone = 2 };
+RL_DEV int trace_next(TraceRay& r, const int32_t* stack) {
+	if (r.leaf_left != 0) return kWorkTriangle;
+	for (;;) {
+		if (r.node == kNoNode) {
+			if (r.sp == 0) return kWorkDone;
+			r.node = stack[--r.sp];
+		}
+		if (r.node >= 0) return kWorkNode;
 		const uint32_t code = (uint32_t) (-(r.node + 1));
 		r.leaf_first = code >> 3;
 		r.leaf_left = code & 7u;
 		r.node = kNoNode;
-		return kTraceContinue;
+		if (r.leaf_left != 0) return kWorkTriangle;
 	}
+}
+
+// One triangle test of the current leaf: kTraceHit or kTraceContinue.
+template <class P> RL_DEV int trace_triangle(const SceneView& s, TraceRay& r) {
+	const bool hit = ray_triangle<P>(r, s.triangles + 3 * (size_t) r.leaf_first);
+	++r.leaf_first;
+	--r.leaf_left;
+	return hit ? kTraceHit : kTraceContinue;
+}
+
+// One inner node: both child boxes, the nearer hit child next and the other
+// pushed.  kTraceContinue, or kTraceMiss with the error recorded when the
+// stack is full.
+RL_DEV int trace_node(const SceneView& s, TraceRay& r, int32_t* stack, uint32_t* error) {
 	const float4* n = s.pairs + 2 + 4 * (size_t) r.node;
 	const float4 lo0 = __ldg(n), hi0 = __ldg(n + 1), lo1 = __ldg(n + 2), hi1 = __ldg(n + 3);
 	float e0, e1;
@@ -178,6 +187,19 @@ template <class P> RL_DEV int trace_step(const SceneView& s, TraceRay& r, int32_
 		r.node = h0 ? ref0 : (h1 ? ref1 : kNoNode);
 	}
 	return kTraceContinue;
+}
+
+// One step: one triangle test or one inner node.  Gives up after
+// kTraversalLimit steps or on a stack overflow, records the error and
+// reports "not occluded".
+template <class P> RL_DEV int trace_step(const SceneView& s, TraceRay& r, int32_t* stack, uint32_t* error) {
+	if (++r.visits > kTraversalLimit) {
+		atomicOr(error, kErrorTraversalLimit);
+		return kTraceMiss;
+	}
+	const int work = trace_next(r, stack);
+	if (work == kWorkDone) return kTraceMiss;
+	return work == kWorkTriangle ? trace_triangle<P>(s, r) : trace_node(s, r, stack, error);
 }
 
 // Any-hit query; true if occluded.
