@@ -264,8 +264,9 @@ typedef enum risltc_numerics_e {
 	/* Hardware reciprocal square root, approximate division and
 	   contraction in the RIS candidate evaluation, whose results only weight
 	   the reservoir; the final PSA/MIS shading stays exact.  Faster; the
-	   estimates stay within 1e-5 relative of the exact path wherever both
-	   choose the same light. */
+	   chosen light equals the exact path's for at least 99.9% of pixels, and
+	   where it does the estimates agree within 1% relative at the 99th
+	   percentile (the tested bounds). */
 	risltc_numerics_fast = 1
 } risltc_numerics_t;
 
@@ -274,6 +275,24 @@ typedef enum risltc_proposal_e {
 	risltc_proposal_clusters = 1, /* cluster weights: power over distance with a cosine bound */
 	risltc_proposal_learned = 2   /* cluster weights: softmax of a learned model's logits */
 } risltc_proposal_t;
+
+/* Tile shapes of the RIS candidate kernel: pixels per warp x candidates per
+   pixel per chunk (the warp sorts each chunk's candidates by vertex count
+   and evaluates them 32 at a time), or one thread per pixel with its
+   candidates in sequence.  In exact numerics every shape gives the same
+   results bit for bit; in fast numerics the binned shapes agree bit for bit
+   and the per-pixel shape, whose multiply-adds the compiler contracts in
+   its own way, agrees within the fast-numerics bounds.  risltc_autotune
+   picks the fastest for a workload. */
+typedef enum risltc_tile_e {
+	risltc_tile_32x8 = 0, /* default */
+	risltc_tile_16x8 = 1,
+	risltc_tile_8x8 = 2,
+	risltc_tile_32x4 = 3,
+	risltc_tile_16x4 = 4,
+	risltc_tile_per_pixel = 5,
+	risltc_tile_count = 6
+} risltc_tile_t;
 
 typedef struct risltc_settings_s {
 	sample_polygon_technique_t polygon_sampling_technique; /* ltc_cp or projected_solid_angle(_biased) */
@@ -291,6 +310,7 @@ typedef struct risltc_settings_s {
 	   risltc_scene_set_clusters mixed with uniform sampling. */
 	risltc_proposal_t proposal;
 	float proposal_uniform_fraction; /* in (0, 1]: weight of the uniform part */
+	risltc_tile_t tile;         /* candidate kernel tile shape (default configuration only) */
 } risltc_settings_t;
 
 /* specify_default_render_settings, src/main.c:220-236 (M = 32, shadows on) */
@@ -453,6 +473,26 @@ typedef struct risltc_batch_item_s {
  * larger items allocate nothing, so a batch can be captured into one CUDA
  * graph. */
 EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* items, uint32_t item_count);
+
+/* Autotuner of the candidate kernel's tile shape: for every risltc_tile_t,
+ * one untimed and `repeats` timed runs of the shading call that `settings`
+ * describes (risltc_shade with these arguments, outputs discarded; the
+ * noise seed is not advanced), timing the candidate kernel with CUDA events
+ * on the context's stream.  Sets settings->tile to the fastest shape and, if
+ * ms_per_tile is not NULL, stores each shape's mean time per call
+ * (risltc_tile_count floats; settings that do not use the candidate kernel
+ * leave settings->tile unchanged and store zeros).  Synchronises the
+ * context's stream. */
+EXTERN_C int risltc_autotune(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                             risltc_settings_t* settings, const noise_table_t* noise, uint32_t frame_count,
+                             uint32_t repeats, float* ms_per_tile);
+
+/* The same for a batch: every shape is timed on the whole risltc_shade_batch
+ * call (CUDA events on the context's stream around the fork and join), the
+ * fastest is written to every item's settings.tile, and the items' noise
+ * seeds are restored.  Synchronises the context's stream. */
+EXTERN_C int risltc_autotune_batch(risltc_ctx_t* ctx, risltc_batch_item_t* items, uint32_t item_count,
+                                   uint32_t repeats, float* ms_per_tile);
 
 /* Same with host buffers: copies the G-buffer planes in, shades, copies
  * out_rgb back, synchronises and reports device errors.  This is the call a

@@ -2,5 +2,5 @@
 lights with an LTC target, projected solid angle sampling, shadow rays, MIS)
 as hand-written CUDA for GB300 (sm_103a) behind a C ABI (include/risltc.h)."""
 from . import api, scenes  # noqa: F401
-from .api import (Context, Scene, Model, RisltcError, settings, shade, shade_batch, shade_host, trace_shadow,  # noqa: F401
-                  noise_constants)
+from .api import (Context, Scene, Model, RisltcError, settings, copy_settings, shade, shade_batch,  # noqa: F401
+                  shade_host, trace_shadow, noise_constants, autotune, autotune_batch)

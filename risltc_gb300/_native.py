@@ -59,7 +59,7 @@ class Settings(ctypes.Structure):
                 ("sample_count", ctypes.c_uint32), ("sample_count_light", ctypes.c_uint32),
                 ("mis_visibility_estimate", ctypes.c_float), ("fast_atan", ctypes.c_uint32),
                 ("shadows", ctypes.c_uint32), ("numerics", ctypes.c_int32), ("proposal", ctypes.c_int32),
-                ("proposal_uniform_fraction", ctypes.c_float)]
+                ("proposal_uniform_fraction", ctypes.c_float), ("tile", ctypes.c_int32)]
 
 
 class GBuffer(ctypes.Structure):
@@ -148,6 +148,11 @@ SIGNATURES = {
                                     ctypes.POINTER(Settings), ctypes.POINTER(NoiseTable), ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "risltc_shade_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_uint32]),
+    "risltc_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer),
+                                       ctypes.POINTER(Settings), ctypes.POINTER(NoiseTable), ctypes.c_uint32,
+                                       ctypes.c_uint32, c_float_p]),
+    "risltc_autotune_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_uint32,
+                                             ctypes.c_uint32, c_float_p]),
     "risltc_shade_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
                                          c_float_p, c_u32_p, ctypes.POINTER(Settings), ctypes.POINTER(NoiseTable),
                                          ctypes.c_uint32, ctypes.c_uint32, c_float_p]),

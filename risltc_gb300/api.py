@@ -20,11 +20,15 @@ MIS_HEURISTICS = {"balance": 0, "power": 1, "weighted": 2, "optimal_clamped": 3,
 LIGHT_SAMPLING = {"uniform": 0, "ris": 1}
 NUMERICS = {"exact": 0, "fast": 1}
 PROPOSALS = {"uniform": 0, "clusters": 1, "learned": 2}
+# risltc_tile_t: candidate kernel tile shapes (pixels per warp x candidates
+# per pixel per chunk, or one thread per pixel), in enum order.
+TILES = {"32x8": 0, "16x8": 1, "8x8": 2, "32x4": 3, "16x4": 4, "per_pixel": 5}
+TILE_NAMES = {v: k for k, v in TILES.items()}
 
 
 def settings(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", candidates=32, sample_count=1,
              light_samples=1, mis_visibility_estimate=0.5, fast_atan=False, shadows=True, numerics="exact",
-             proposal="uniform", proposal_uniform_fraction=0.1):
+             proposal="uniform", proposal_uniform_fraction=0.1, tile="32x8"):
     """risltc_settings_t; defaults are specify_default_render_settings
     (src/main.c:220-236) with the reference's hard-coded M = 32."""
     s = _native.Settings()
@@ -41,7 +45,17 @@ def settings(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", ca
     s.numerics = NUMERICS[numerics]
     s.proposal = PROPOSALS[proposal]
     s.proposal_uniform_fraction = proposal_uniform_fraction
+    s.tile = TILES[tile]
     return s
+
+
+def copy_settings(s, **changes):
+    """A copy of risltc_settings_t s with fields replaced (tile by name)."""
+    out = _native.Settings()
+    ctypes.pointer(out)[0] = s
+    for k, v in changes.items():
+        setattr(out, k, TILES[v] if k == "tile" else v)
+    return out
 
 
 def noise_constants(frame, animate=True):
@@ -233,12 +247,7 @@ def shade(ctx, scene, gbuffer, width, height, s, noise_seed=0, animate=True, fra
     return nt.random_seed
 
 
-def shade_batch(ctx, items):
-    """risltc_shade_batch.  items: dicts with the keyword arguments of shade()
-    (scene, gbuffer, width, height, settings, noise_seed, animate, frames,
-    out_rgb, accum, reservoirs, primitive).  Returns each item's next noise
-    seed."""
-    lib = _native.load()
+def _batch_array(items):
     arr = (_native.BatchItem * len(items))()
     tables = [_native.NoiseTable(it.get("noise_seed", 0)) for it in items]
     ptr = (lambda t: None if t is None else t.data_ptr())
@@ -251,8 +260,44 @@ def shade_batch(ctx, items):
         a.animate = int(it.get("animate", True))
         a.frame_count = it.get("frames", 1)
         a.out_rgb, a.accum, a.reservoirs = ptr(it.get("out_rgb")), ptr(it.get("accum")), ptr(it.get("reservoirs"))
-    check(lib.risltc_shade_batch(ctx.handle, arr, len(items)), "risltc_shade_batch")
+    return arr, tables
+
+
+def shade_batch(ctx, items):
+    """risltc_shade_batch.  items: dicts with the keyword arguments of shade()
+    (scene, gbuffer, width, height, settings, noise_seed, animate, frames,
+    out_rgb, accum, reservoirs, primitive).  Returns each item's next noise
+    seed."""
+    arr, tables = _batch_array(items)
+    check(_native.load().risltc_shade_batch(ctx.handle, arr, len(items)), "risltc_shade_batch")
     return [nt.random_seed for nt in tables]
+
+
+def autotune(ctx, scene, gbuffer, width, height, s, noise_seed=0, frames=1, repeats=3, primitive=None):
+    """risltc_autotune: times the candidate kernel of this shade() call with
+    every tile shape.  Returns (a copy of s with the fastest tile, {tile name:
+    mean ms per call})."""
+    lib = _native.load()
+    g = _native.GBuffer(width, height, gbuffer.data_ptr(), None if primitive is None else primitive.data_ptr())
+    tuned = copy_settings(s)
+    nt = _native.NoiseTable(noise_seed)
+    ms = (ctypes.c_float * len(TILES))()
+    check(lib.risltc_autotune(ctx.handle, scene.handle, ctypes.byref(g), ctypes.byref(tuned), ctypes.byref(nt),
+                              frames, repeats, ms), "risltc_autotune")
+    return tuned, {TILE_NAMES[t]: ms[t] for t in range(len(TILES))}
+
+
+def autotune_batch(ctx, items, repeats=3):
+    """risltc_autotune_batch: times the whole shade_batch(ctx, items) call with
+    every tile shape and stores a copy of each item's settings with the
+    fastest tile in items[i]["settings"].  Returns (tile name, {tile name:
+    mean ms per batch})."""
+    arr, _ = _batch_array(items)
+    ms = (ctypes.c_float * len(TILES))()
+    check(_native.load().risltc_autotune_batch(ctx.handle, arr, len(items), repeats, ms), "risltc_autotune_batch")
+    for it, a in zip(items, arr):
+        it["settings"] = copy_settings(a.settings)
+    return TILE_NAMES[arr[0].settings.tile], {TILE_NAMES[t]: ms[t] for t in range(len(TILES))}
 
 
 def shade_host(ctx, scene, gbuffer, width, height, s, noise_seed=0, animate=True, frames=1, primitive=None,

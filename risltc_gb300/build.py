@@ -17,12 +17,17 @@ LIB = os.path.join(PKG, "librisltc_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["host/light.c", "host/ltc_table.c", "host/bvh.c", "host/quicksave.c", "host/clusters.c"]
-CUDA_SOURCES = {
-    "cuda/shade_exact.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
-    "cuda/shade_fast.cu": ["--fmad=true", "-prec-div=true", "-prec-sqrt=true"],
-    "cuda/api.cu": [],
-    "cuda/noalloc.cu": [],
-}
+EXACT = ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"]
+FAST = ["--fmad=true", "-prec-div=true", "-prec-sqrt=true"]
+# (source, flags, object): candidate_tiles.cu is built once per numerics mode.
+CUDA_SOURCES = [
+    ("cuda/shade_exact.cu", EXACT, "shade_exact.o"),
+    ("cuda/shade_fast.cu", FAST, "shade_fast.o"),
+    ("cuda/candidate_tiles.cu", EXACT + ["-DRISLTC_TILE_FAST=0"], "candidate_tiles_exact.o"),
+    ("cuda/candidate_tiles.cu", FAST + ["-DRISLTC_TILE_FAST=1"], "candidate_tiles_fast.o"),
+    ("cuda/api.cu", [], "api.o"),
+    ("cuda/noalloc.cu", [], "noalloc.o"),
+]
 
 
 def nvcc():
@@ -61,8 +66,8 @@ def build(force=False, verbose=False, extra_flags=(), out=None):
         obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         jobs.append((["gcc", "-std=c99", "-O3", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
                       "-c", os.path.join(CSRC, src), "-o", obj], obj))
-    for src, flags in CUDA_SOURCES.items():
-        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
+    for src, flags, name in CUDA_SOURCES:
+        obj = os.path.join(build_dir, name)
         cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                "-Xptxas", "-v"] + ARCH + flags + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
         jobs.append((cmd, obj))

@@ -12,6 +12,11 @@
 #include "ris_binned.cuh"
 #include "ris_wavefront.cuh"
 
+// Triangles per BVH leaf before the SAH is consulted.
+#ifndef RISLTC_BVH_LEAF
+#define RISLTC_BVH_LEAF 4
+#endif
+
 namespace risltc {
 cudaError_t launch_proposal(const ProposalParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast);
@@ -338,7 +343,7 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	risltc_bvh_t bvh;
 	memset(&bvh, 0, sizeof(bvh));
 	if (triangle_count) {
-		int st = risltc_bvh_build(&bvh, triangles, triangle_count, 4);
+		int st = risltc_bvh_build(&bvh, triangles, triangle_count, RISLTC_BVH_LEAF);
 		if (st) return st;
 	}
 	risltc_scene_t* scene = (risltc_scene_t*) calloc(1, sizeof(risltc_scene_t));
@@ -474,6 +479,7 @@ static int validate_settings(const risltc_settings_t* s) {
 	    s->sample_count_light < 1 || s->sample_count_light > 64)
 		return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (s->numerics != risltc_numerics_exact && s->numerics != risltc_numerics_fast) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if ((int) s->tile < 0 || s->tile >= risltc_tile_count) return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (s->proposal != risltc_proposal_uniform && s->proposal != risltc_proposal_clusters &&
 	    s->proposal != risltc_proposal_learned)
 		return RISLTC_ERROR_INVALID_ARGUMENT;
@@ -772,7 +778,7 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		r.reservoirs = reservoirs;
 		r.error = ctx->d_error;
 		e = risltc::launch_ris(r, stream, grid_for(ctx, pixels), grid_for(ctx, 2 * pixels * frame_count), events,
-		                       fast);
+		                       fast, (int) settings->tile, ctx->sm_count * 16);
 		if (e == cudaSuccess && train)
 			e = launch_training(ctx, stream, scene, gbuffer, sc.candidates, r.candidate_count, r.train_stride,
 			                    r.train_phase, r.train_shaded, r.records);
@@ -784,15 +790,24 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 
 }  // namespace
 
-EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
-                          const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
-                          uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs) {
+namespace {
+
+int check_shade_call(const risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                     const risltc_settings_t* settings, const noise_table_t* noise, uint32_t frame_count) {
 	if (!ctx || !valid_call(scene, gbuffer, noise, frame_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	int st = validate_settings(settings);
 	if (st) return st;
 	if (uses_proposal(settings) && scene->clusters.count == 0) return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (settings->proposal == risltc_proposal_learned && !scene->model) return RISLTC_ERROR_INVALID_ARGUMENT;
-	cudaSetDevice(ctx->device);
+	return RISLTC_OK;
+}
+
+// risltc_shade after its checks: grows the scratch and launches on the
+// context's stream with the given events (may be null).
+int shade_on_context(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                     const risltc_settings_t* settings, uint32_t noise_seed, uint32_t animate, uint32_t frame_count,
+                     float* out_rgb, double* accum, risltc_reservoir_t* reservoirs, cudaEvent_t* events) {
+	int st;
 	const size_t pixel_frames = (size_t) gbuffer->width * gbuffer->height * frame_count;
 	if (uses_proposal(settings) && (st = reserve_candidates(ctx, pixel_frames * settings->candidate_count)))
 		return st;
@@ -806,6 +821,20 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		    (st = reserve_wavefront(ctx, pixel_frames, scene->view.light_count)))
 			return st;
 	}
+	const Scratch sc{ctx->d_records, ctx->d_phat, ctx->d_candidates, ctx->d_logits, ctx->d_samples, ctx->d_staged,
+	                 ctx->d_rays, ctx->d_hits, ctx->d_ray_count, ctx->d_light_rays};
+	return shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise_seed, animate, frame_count, out_rgb, accum,
+	                 reservoirs, events);
+}
+
+}  // namespace
+
+EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                          const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,
+                          uint32_t frame_count, float* out_rgb, double* accum, risltc_reservoir_t* reservoirs) {
+	int st = check_shade_call(ctx, scene, gbuffer, settings, noise, frame_count);
+	if (st) return st;
+	cudaSetDevice(ctx->device);
 	cudaEvent_t* events = nullptr;
 	if (ctx->profiling && ctx->timed_calls < 64) {
 		int i = ctx->timed_calls++;
@@ -815,12 +844,125 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 		}
 		events = ctx->events[i];
 	}
-	const Scratch sc{ctx->d_records, ctx->d_phat, ctx->d_candidates, ctx->d_logits, ctx->d_samples, ctx->d_staged,
-	                 ctx->d_rays, ctx->d_hits, ctx->d_ray_count, ctx->d_light_rays};
-	st = shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise->random_seed, animate, frame_count, out_rgb,
-	               accum, reservoirs, events);
+	st = shade_on_context(ctx, scene, gbuffer, settings, noise->random_seed, animate, frame_count, out_rgb, accum,
+	                      reservoirs, events);
 	if (st) return st;
 	noise->random_seed += frame_count;
+	return RISLTC_OK;
+}
+
+namespace {
+
+// Five timing events for the autotuner, destroyed with the object.
+struct TuneEvents {
+	cudaEvent_t e[5] = {};
+	int created = 0;
+	cudaError_t create() {
+		for (; created != 5; ++created) {
+			cudaError_t r = cudaEventCreate(&e[created]);
+			if (r != cudaSuccess) return r;
+		}
+		return cudaSuccess;
+	}
+	~TuneEvents() {
+		for (int k = 0; k != created; ++k) cudaEventDestroy(e[k]);
+	}
+};
+
+int fastest_tile(const float* ms) {
+	int best = 0;
+	for (int t = 1; t != risltc_tile_count; ++t)
+		if (ms[t] < ms[best]) best = t;
+	return best;
+}
+
+}  // namespace
+
+EXTERN_C int risltc_autotune(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                             risltc_settings_t* settings, const noise_table_t* noise, uint32_t frame_count,
+                             uint32_t repeats, float* ms_per_tile) {
+	int st = check_shade_call(ctx, scene, gbuffer, settings, noise, frame_count);
+	if (st) return st;
+	if (repeats == 0 || repeats > 1000) return RISLTC_ERROR_INVALID_ARGUMENT;
+	float ms[risltc_tile_count] = {};
+	if (uses_ris_pipeline(settings)) {
+		cudaSetDevice(ctx->device);
+		TuneEvents ev;
+		cudaError_t e = ev.create();
+		if (e != cudaSuccess) return cuda_status(e);
+		risltc_settings_t s = *settings;
+		for (int t = 0; t != risltc_tile_count; ++t) {
+			s.tile = (risltc_tile_t) t;
+			for (uint32_t r = 0; r <= repeats; ++r) {
+				st = shade_on_context(ctx, scene, gbuffer, &s, noise->random_seed, 1, frame_count, nullptr, nullptr,
+				                      nullptr, ev.e);
+				if (st) return st;
+				if ((e = cudaEventSynchronize(ev.e[4])) != cudaSuccess) return cuda_status(e);
+				float candidates = 0.0f;
+				if ((e = cudaEventElapsedTime(&candidates, ev.e[0], ev.e[1])) != cudaSuccess) return cuda_status(e);
+				if (r > 0) ms[t] += candidates / (float) repeats;
+			}
+		}
+		settings->tile = (risltc_tile_t) fastest_tile(ms);
+	}
+	if (ms_per_tile)
+		for (int t = 0; t != risltc_tile_count; ++t) ms_per_tile[t] = ms[t];
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_autotune_batch(risltc_ctx_t* ctx, risltc_batch_item_t* items, uint32_t item_count,
+                                   uint32_t repeats, float* ms_per_tile) {
+	if (!ctx || (!items && item_count) || repeats == 0 || repeats > 1000) return RISLTC_ERROR_INVALID_ARGUMENT;
+	float ms[risltc_tile_count] = {};
+	bool tiled = false;
+	for (uint32_t i = 0; i != item_count; ++i) {
+		if (!items[i].noise) return RISLTC_ERROR_INVALID_ARGUMENT;
+		int st = validate_settings(&items[i].settings);
+		if (st) return st;
+		tiled = tiled || uses_ris_pipeline(&items[i].settings);
+	}
+	if (tiled) {
+		cudaSetDevice(ctx->device);
+		TuneEvents ev;
+		cudaError_t e = ev.create();
+		if (e != cudaSuccess) return cuda_status(e);
+		std::vector<uint32_t> seeds(item_count);
+		std::vector<risltc_tile_t> tiles(item_count);
+		for (uint32_t i = 0; i != item_count; ++i) {
+			seeds[i] = items[i].noise->random_seed;
+			tiles[i] = items[i].settings.tile;
+		}
+		// Puts back the seeds the batch calls advanced (items may share a
+		// noise table) and, on failure, the tiles.
+		auto restore = [&](bool tiles_too) {
+			for (uint32_t i = 0; i != item_count; ++i) {
+				items[i].noise->random_seed = seeds[i];
+				if (tiles_too) items[i].settings.tile = tiles[i];
+			}
+		};
+		for (int t = 0; t != risltc_tile_count; ++t) {
+			for (uint32_t i = 0; i != item_count; ++i) items[i].settings.tile = (risltc_tile_t) t;
+			for (uint32_t r = 0; r <= repeats; ++r) {
+				e = cudaEventRecord(ev.e[0], ctx->stream);
+				int st = e == cudaSuccess ? risltc_shade_batch(ctx, items, item_count) : cuda_status(e);
+				restore(false);
+				if (st == RISLTC_OK && (e = cudaEventRecord(ev.e[1], ctx->stream)) != cudaSuccess) st = cuda_status(e);
+				if (st == RISLTC_OK && (e = cudaEventSynchronize(ev.e[1])) != cudaSuccess) st = cuda_status(e);
+				float call = 0.0f;
+				if (st == RISLTC_OK && (e = cudaEventElapsedTime(&call, ev.e[0], ev.e[1])) != cudaSuccess)
+					st = cuda_status(e);
+				if (st) {
+					restore(true);
+					return st;
+				}
+				if (r > 0) ms[t] += call / (float) repeats;
+			}
+		}
+		const int best = fastest_tile(ms);
+		for (uint32_t i = 0; i != item_count; ++i) items[i].settings.tile = (risltc_tile_t) best;
+	}
+	if (ms_per_tile)
+		for (int t = 0; t != risltc_tile_count; ++t) ms_per_tile[t] = ms[t];
 	return RISLTC_OK;
 }
 

@@ -99,7 +99,9 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 	size_t blocks = ((size_t) gbuffer->width * gbuffer->height + 127) / 128;
 	if (blocks > (size_t) sms * 16) blocks = (size_t) sms * 16;
-	e = risltc::launch_ris(r, s, (int) blocks, (int) blocks, nullptr, settings->numerics == risltc_numerics_fast);
+	// No p_hat scratch: the candidate kernel with one thread per pixel.
+	e = risltc::launch_ris(r, s, (int) blocks, (int) blocks, nullptr, settings->numerics == risltc_numerics_fast,
+	                       risltc_tile_per_pixel, sms * 16);
 	if (e != cudaSuccess) return to_status(e);
 	uint32_t bits = 0;
 	e = cudaMemcpyAsync(&bits, &scratch->error, sizeof(bits), cudaMemcpyDeviceToHost, s);

@@ -1,8 +1,10 @@
 // ris_binned.cuh - the RIS candidate phase as a warp-per-tile kernel with
 // work binning.
 //
-// Each warp owns 32 consecutive pixels and takes their candidates in
-// super-chunks of kSuper, each made of chunks of kChunk.  Per chunk the warp
+// Each warp owns kPixels consecutive pixels (32, 16 or 8: the tile's pixels
+// per warp) and takes their candidates in super-chunks of kSuper, each made
+// of chunks of kChunk (the tile's candidates per pixel per chunk; 8 or 4).
+// Per chunk the warp
 //   1. draws every pixel's candidate lights from that pixel's noise stream
 //      (the LCG sequence of shading_pass.frag.glsl:728-736: a light draw, then
 //      the reservoir draw, per candidate);
@@ -21,25 +23,20 @@
 // ris_candidates_kernel and the reservoir sees them in the same order, so the
 // reservoir records are bit-identical.
 #pragma once
+#include <algorithm>
 #include <atomic>
 #include "ris_kernels.cuh"
 
 namespace risltc {
 
-#ifndef RISLTC_BINNED_CHUNK
-#define RISLTC_BINNED_CHUNK 8
-#endif
 #ifndef RISLTC_BINNED_MIN_BLOCKS
 #define RISLTC_BINNED_MIN_BLOCKS 4
 #endif
-constexpr int kChunk = RISLTC_BINNED_CHUNK;  // candidates per pixel per chunk
-constexpr int kItems = 32 * kChunk;          // items per warp per chunk
 // A warp's p_hat values of one super-chunk, [pixel lane][candidate], live in
 // its slot of RisParams::p_hat_scratch (global memory, L2/L1): keeping them
 // out of shared memory leaves room in the SM's combined L1/shared storage
 // for the light records the candidates read.
 constexpr int kPHatSlot = 32 * 32;
-constexpr int kDeferred = kItems + 32;       // deferred items pending at most
 
 // Candidates per pixel per super-chunk (measured best: 32 in exact numerics,
 // 16 in fast numerics, where the smaller tile leaves more L1 for the lights).
@@ -55,11 +52,13 @@ template <> struct BinnedSuper<FastNumerics> {
 constexpr int kFrameWords = 45;              // 44 used; odd stride avoids bank conflicts
 constexpr int kBinnedWarps = 4;              // warps per block
 constexpr int kBins = kMaxLightVertices - 2; // vertex counts 3..8
-static_assert(kItems < 1024, "10-bit bin counters");
 
-template <int kSuper> struct WarpTile {
-	static_assert(kSuper % kChunk == 0 && 32 * kSuper <= 65536, "super-chunk layout");
-	float frame[32][kFrameWords];
+template <int kSuper, int kPixels, int kChunk> struct WarpTile {
+	static constexpr int kItems = kPixels * kChunk;  // items per warp per chunk
+	static constexpr int kDeferred = kItems + 32;     // deferred items pending at most
+	static_assert(kItems < 1024, "10-bit bin counters");
+	static_assert(kSuper % kChunk == 0 && kPixels * kSuper <= kPHatSlot, "super-chunk layout");
+	float frame[kPixels][kFrameWords];
 	// Items as light << 10 | slot, slot = pixel lane * kSuper + candidate of
 	// the super-chunk (below 1024; lights below 2^22).
 	uint32_t item[kItems];
@@ -188,23 +187,26 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 	return true;
 }
 
-template <class P>
+template <class P, int kPixels, int kChunk>
 __global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
 ris_candidates_binned_kernel(RisParams pr) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	constexpr int kSuper = BinnedSuper<P>::value;
-	static_assert(32 * kSuper <= kPHatSlot, "p_hat slot");
-	WarpTile<kSuper>& tile = reinterpret_cast<WarpTile<kSuper>*>(smem_raw)[threadIdx.x / 32];
+	using Tile = WarpTile<kSuper, kPixels, kChunk>;
+	Tile& tile = reinterpret_cast<Tile*>(smem_raw)[threadIdx.x / 32];
 	float* const phat = pr.p_hat_scratch + (size_t) (blockIdx.x * kBinnedWarps + threadIdx.x / 32) * kPHatSlot;
 	const uint32_t lane = threadIdx.x % 32;
 	const uint32_t np = pr.width * pr.height;
 	const int n_lights = pr.scene.light_count;
 	const float p = P::rcp((float) n_lights);
 	const uint32_t warps_total = gridDim.x * kBinnedWarps;
-	const uint32_t tiles = (np + 31) / 32;
+	const uint32_t tiles = (np + kPixels - 1) / kPixels;
+	// Lanes kPixels..31 own no pixel: they draw nothing and only evaluate
+	// items of the sorted lists.
+	const bool own = lane < (uint32_t) kPixels;
 	for (uint32_t t = blockIdx.x * kBinnedWarps + threadIdx.x / 32; t < tiles; t += warps_total) {
-		const uint32_t i = t * 32 + lane;
-		const bool valid = i < np && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
+		const uint32_t i = t * kPixels + lane;
+		const bool valid = own && i < np && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
 		if (valid) {
 			const float* g = pr.gbuffer;
 			const size_t snp = np;
@@ -365,26 +367,31 @@ ris_candidates_binned_kernel(RisParams pr) {
 			}
 			if (valid)
 				pr.records[(size_t) f * np + i] = ReservoirRecord{res_index, w_sum, sample_value, seed};
-			else if (i < np)
+			else if (own && i < np)
 				pr.records[(size_t) f * np + i] = ReservoirRecord{-1, 0.0f, 0.0f, 0u};
 		}
 		__syncwarp();
 	}
 }
 
-template <class P> constexpr size_t binned_smem_bytes() {
-	return sizeof(WarpTile<BinnedSuper<P>::value>) * kBinnedWarps;
+template <class P, int kPixels, int kChunk> constexpr size_t binned_smem_bytes() {
+	return sizeof(WarpTile<BinnedSuper<P>::value, kPixels, kChunk>) * kBinnedWarps;
 }
 
 // Launches the binned candidate kernel.  Its shared memory exceeds the 48 KB
 // available without opting in, so the limit is raised the first time the
 // kernel runs on a device (once, so that later launches, including those
 // captured into a CUDA graph, make no other runtime call).
-template <class P> cudaError_t launch_candidates_binned(const RisParams& p, cudaStream_t stream, int grid) {
+// grid_cap is the largest grid the p_hat scratch has warp slots for.
+template <class P, int kPixels, int kChunk>
+cudaError_t launch_candidates_binned(const RisParams& p, cudaStream_t stream, int grid_cap) {
+	const size_t pixels = (size_t) p.width * p.height;
+	const size_t blocks = (pixels + kPixels * kBinnedWarps - 1) / (kPixels * kBinnedWarps);
+	const int grid = (int) std::max<size_t>(1, std::min<size_t>(blocks, (size_t) grid_cap));
 	// Without p_hat scratch (the allocation-free entry point), the kernel with
 	// one thread per pixel computes the same records.
 	if (!p.p_hat_scratch) {
-		ris_candidates_kernel<P><<<grid, 128, 0, stream>>>(p);
+		ris_candidates_kernel<P><<<grid_for_pixels(pixels, grid_cap), 128, 0, stream>>>(p);
 		return cudaGetLastError();
 	}
 	static std::atomic<uint64_t> configured{0};
@@ -393,12 +400,13 @@ template <class P> cudaError_t launch_candidates_binned(const RisParams& p, cuda
 	if (e != cudaSuccess) return e;
 	const uint64_t bit = 1ull << (device & 63);
 	if (!(configured.load() & bit)) {
-		e = cudaFuncSetAttribute(ris_candidates_binned_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                         (int) binned_smem_bytes<P>());
+		e = cudaFuncSetAttribute(ris_candidates_binned_kernel<P, kPixels, kChunk>,
+		                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int) binned_smem_bytes<P, kPixels, kChunk>());
 		if (e != cudaSuccess) return e;
 		configured.fetch_or(bit);
 	}
-	ris_candidates_binned_kernel<P><<<grid, 32 * kBinnedWarps, binned_smem_bytes<P>(), stream>>>(p);
+	ris_candidates_binned_kernel<P, kPixels, kChunk>
+	    <<<grid, 32 * kBinnedWarps, binned_smem_bytes<P, kPixels, kChunk>(), stream>>>(p);
 	return cudaGetLastError();
 }
 

@@ -307,23 +307,37 @@ template <class P> __global__ void __launch_bounds__(128) ris_shade_kernel(RisPa
 	}
 }
 
-cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid);
-cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid);
+// Blocks of 128 threads for one thread per pixel, at most grid_cap.
+inline int grid_for_pixels(size_t pixels, int grid_cap) {
+	const size_t blocks = (pixels + 127) / 128;
+	return (int) (blocks == 0 ? 1 : (blocks < (size_t) grid_cap ? blocks : (size_t) grid_cap));
+}
+
+// The candidate kernel with the tile shape `tile` (a risltc_tile_t); grid_cap
+// is the largest grid the p_hat scratch has warp slots for.  The default and
+// per-pixel shapes live with the other kernels of each numerics mode, the
+// rest in their own translation units (launch_candidates_tile_*).
+cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid_cap, int tile);
+cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid_cap, int tile);
+cudaError_t launch_candidates_tile_exact(const RisParams& p, cudaStream_t stream, int grid_cap, int tile);
+cudaError_t launch_candidates_tile_fast(const RisParams& p, cudaStream_t stream, int grid_cap, int tile);
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_ris_sample(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_shadow_sort(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_shadow_trace(const RisParams& p, cudaStream_t stream, int grid);
 cudaError_t launch_ris_resolve(const RisParams& p, cudaStream_t stream, int grid);
 
-// The candidate kernel (fast or exact numerics), then the shading phase
-// (always exact): ris_shade_kernel, or with p.samples set the sample kernel,
-// the shadow rays' grouping by light and trace, and the resolve kernel.  events (may be null) holds five events,
+// The candidate kernel (fast or exact numerics, tile shape `tile`, at most
+// grid_cap blocks), then the shading phase (always exact): ris_shade_kernel,
+// or with p.samples set the sample kernel, the shadow rays' grouping by light
+// and trace, and the resolve kernel.  events (may be null) holds five events,
 // recorded before, between and after the phases (the last three together for
 // ris_shade_kernel).
 inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid, int trace_grid, cudaEvent_t* events,
-                              bool fast) {
+                              bool fast, int tile, int grid_cap) {
 	if (events) cudaEventRecord(events[0], stream);
-	cudaError_t e = fast ? launch_candidates_fast(p, stream, grid) : launch_candidates_exact(p, stream, grid);
+	cudaError_t e = fast ? launch_candidates_fast(p, stream, grid_cap, tile)
+	                     : launch_candidates_exact(p, stream, grid_cap, tile);
 	if (e != cudaSuccess) return e;
 	if (events) cudaEventRecord(events[1], stream);
 	if (p.samples) {

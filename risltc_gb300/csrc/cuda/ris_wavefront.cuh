@@ -269,6 +269,9 @@ static __global__ void __launch_bounds__(128) shadow_scatter_kernel(RisParams pr
 	}
 }
 
+#ifndef RISLTC_TRACE_MIN_BLOCKS
+#define RISLTC_TRACE_MIN_BLOCKS 1
+#endif
 #ifndef RISLTC_TRACE_REFILL
 #define RISLTC_TRACE_REFILL 8
 #endif
@@ -278,7 +281,7 @@ static __global__ void __launch_bounds__(128) shadow_scatter_kernel(RisParams pr
 // whenever RISLTC_TRACE_REFILL or more lanes of a warp are idle they fetch
 // the next rays together, so lanes do not wait for the warp's longest ray.
 template <class P>
-__global__ void __launch_bounds__(128) shadow_trace_kernel(SceneView s, const ShadowRay* rays, uint32_t* queue,
+__global__ void __launch_bounds__(128, RISLTC_TRACE_MIN_BLOCKS) shadow_trace_kernel(SceneView s, const ShadowRay* rays, uint32_t* queue,
                                                            uint8_t* hits, uint32_t* error) {
 	const uint32_t n = queue[0];
 	const uint32_t lane = threadIdx.x % 32;

@@ -17,8 +17,14 @@ cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cu
 		for (int k = 1; k != 5; ++k) cudaEventRecord(events[k], stream);
 	return e;
 }
-cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid) {
-	return launch_candidates_binned<ExactNumerics>(p, stream, grid);
+cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid_cap, int tile) {
+	if (tile == risltc_tile_32x8) return launch_candidates_binned<ExactNumerics, 32, 8>(p, stream, grid_cap);
+	if (tile == risltc_tile_per_pixel) {
+		ris_candidates_kernel<ExactNumerics>
+		    <<<grid_for_pixels((size_t) p.width * p.height, grid_cap), 128, 0, stream>>>(p);
+		return cudaGetLastError();
+	}
+	return launch_candidates_tile_exact(p, stream, grid_cap, tile);
 }
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid) {
 	ris_shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);

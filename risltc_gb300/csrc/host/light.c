@@ -168,4 +168,5 @@ void risltc_default_settings(risltc_settings_t* s) {
 	s->numerics = risltc_numerics_exact;
 	s->proposal = risltc_proposal_uniform;
 	s->proposal_uniform_fraction = 0.1f;
+	s->tile = risltc_tile_32x8;
 }
