@@ -48,36 +48,50 @@ struct ShadowRay {
 };
 
 // evaluate_polygonal_light_shading_peters for SAMPLE_COUNT == 1 up to the
-// visibility test.  Returns the two techniques' modes; fills c and ray.
+// visibility test.  Returns the two techniques' modes; fills c and ray.  l
+// is the light whose device record is `record`.
 template <class P>
-RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l, uint32_t& seed,
-                             f3 (&c)[2][2], ShadowRay (&ray)[2]) {
+RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l,
+                             const float4* record, uint32_t& seed, f3 (&c)[2][2], ShadowRay (&ray)[2]) {
 	const bool fa = pr.fast_atan != 0;
 	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
-	PsaPolygon pd, ps;
-	if (!psa_prepare_both<P>(pr, sd, ltc, l, pd, ps)) return 0;
-	float specular_weight = ltc.albedo * ps.psa;
-	f3 diffuse_weight = scale(max3(sd.diffuse_albedo, splat(0.01f)), pd.psa);
-	int technique_count = (ps.psa > 0.0f) ? 2 : 1;
-	float rcp_d = P::rcp(pd.psa);
-	float rcp_s = P::rcp(ps.psa);
+	side_flip(ltc, sd, l);
+	// One polygon buffer serves both spaces: the shading-space polygon is
+	// prepared and sampled, then the cosine-space one is prepared into the
+	// same storage and sampled (if it has a projected solid angle).  The
+	// samples draw the noise in the reference's order (diffuse, then
+	// specular), and after sampling only the projected solid angles are
+	// needed, so the values equal those of psa_prepare_both followed by both
+	// samples.
+	PsaPolygon poly;
+	float psa[2] = {0.0f, 0.0f};
+	int technique_count = 1;
+	f3 dir_d = mk3(0.0f, 0.0f, 1.0f), dir_s = mk3(0.0f, 0.0f, 1.0f);
+#pragma unroll 1
+	for (int j = 0; j != 2; ++j) {
+		const uint32_t vc = prepare_space_record<P>(j == 0 ? ltc.world_to_shading
+		                                                  : mul(ltc.shading_to_cosine, ltc.world_to_shading),
+		                                           record, poly, fa);
+		psa[j] = vc == 0 ? 0.0f : poly.psa;
+		if (j == 0 && (vc == 0 || psa[0] == 0.0f)) return 0;
+		if (j == 1 && !(psa[1] > 0.0f)) break;
+		const f3 dir = sample_psa<P>(poly, get_noise_2(seed), fa, biased);
+		if (j == 0) {
+			dir_d = dir;
+		} else {
+			dir_s = normalize<P>(mul(ltc.cosine_to_shading, dir));
+			technique_count = 2;
+		}
+	}
+	float specular_weight = ltc.albedo * psa[1];
+	f3 diffuse_weight = scale(max3(sd.diffuse_albedo, splat(0.01f)), psa[0]);
+	float rcp_d = P::rcp(psa[0]);
+	float rcp_s = P::rcp(psa[1]);
 	f3 specular_weight_rgb = splat(specular_weight);
 	if (pr.mis_heuristic == mis_heuristic_optimal) {
 		f3 rop = scale(l.radiance, kInvPi);
 		diffuse_weight = mul(diffuse_weight, rop);
 		specular_weight_rgb = mul(specular_weight_rgb, rop);
-	}
-	// Both samples come from one copy of the sampling code: the diffuse
-	// sample from pd, then (if the specular polygon has a projected solid
-	// angle) the specular one from ps, in the reference's noise order.
-	f3 dir_d = mk3(0.0f, 0.0f, 1.0f), dir_s = mk3(0.0f, 0.0f, 1.0f);
-#pragma unroll 1
-	for (int j = 0; j != technique_count; ++j) {
-		const f3 dir = sample_psa<P>(j == 0 ? pd : ps, get_noise_2(seed), fa, biased);
-		if (j == 0)
-			dir_d = dir;
-		else
-			dir_s = normalize<P>(mul(ltc.cosine_to_shading, dir));
 	}
 	const bool shadows = pr.shadows && pr.scene.triangle_count != 0;
 	uint32_t modes = 0;
@@ -103,7 +117,7 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 			const bool visibility = (o == 0) ? side : false;
 			f3 integrand = scale(visibility ? rb_lit : splat(0.0f), dir.z);
 			f3 r;
-			if (j == 0 && ps.psa <= 0.0f)
+			if (j == 0 && psa[1] <= 0.0f)
 				r = visibility ? scale(integrand, P::rcp(diffuse_density)) : splat(0.0f);
 			else
 				r = mis_estimate<P>(pr.mis_heuristic, integrand, own_weight, own_density, other_weight, other_density,
@@ -182,7 +196,7 @@ template <class P> __global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOC
 					Light l;
 					load_light(pr.scene, r.light_index, l);
 					uint32_t seed = r.seed;
-					modes = psa_mis_emit<P>(sp, sd, ltc, l, seed, c, ray);
+					modes = psa_mis_emit<P>(sp, sd, ltc, l, light_record(pr.scene, r.light_index), seed, c, ray);
 					W = P::div(r.w_sum, (float) pr.candidate_count * r.p_hat);
 					if (r.p_hat == 0.0f) W = 0.0f;
 					flags = modes;

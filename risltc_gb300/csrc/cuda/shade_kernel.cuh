@@ -270,6 +270,25 @@ __device__ __noinline__ uint32_t prepare_space(mat43 w2l, const Light& l, PsaPol
 	return vc;
 }
 
+// prepare_space with the vertices read from the light's device record
+// (the same values as load_light gives), so that callers need not keep a
+// Light in memory for the call.
+template <class P>
+__device__ __noinline__ uint32_t prepare_space_record(mat43 w2l, const float4* record, PsaPolygon& p, bool fa) {
+	const uint32_t n = __float_as_uint(__ldg(record).w);
+	f3 verts[kMaxPolygonVertices];
+#pragma unroll
+	for (int j = 0; j != kMaxLightVertices; ++j) {
+		if (j < (int) n) {
+			const float4 q = __ldg(record + 2 + j);
+			verts[j] = mul_point(w2l, mk3(q.x, q.y, q.z));
+		}
+	}
+	const uint32_t vc = clip_polygon<P>(n, verts);
+	if (vc != 0) prepare_psa<P>(p, vc, verts, fa);
+	return vc;
+}
+
 // The side flip and both polygons' PSA sampling preparations of
 // evaluate_polygonal_light_shading_peters (shading_pass.frag.glsl:298-341):
 // pd in shading space, ps in cosine space.  Returns false when the estimate
