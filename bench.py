@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--reference-spp", type=int, default=4096)
     p.add_argument("--shadowed-target", type=float, default=0.5,
                    help="weight of the shadowed (visibility) part of the learned proposal's training target")
+    p.add_argument("--sweep-candidates", default="",
+                   help="equal-mse: also measure every method at these candidate counts (comma-separated); plain "
+                        "RIS at --candidates stays the MSE level to reach")
     return p.parse_args()
 
 
@@ -397,7 +400,8 @@ def run_equal_mse(a):
     trains online for a.train_frames frames first (1 spp each, every 16th
     pixel); then each method renders a.spp spp four times with fresh noise
     and its MSE against the reference is measured, with its device time per
-    frame (CUDA events, training off).  MSE falls as 1 / spp for these
+    frame (CUDA events over a.steps calls of a.spp frames each, the same
+    calls that the MSE is measured on; training off).  MSE falls as 1 / spp for these
     unbiased estimators, so the time to reach plain RIS's a.spp-spp MSE is
     ms_per_frame * spp * MSE(method) / MSE(plain)."""
     import torch
@@ -443,7 +447,11 @@ def run_equal_mse(a):
     train_ms = t0.elapsed_time(t1) / max(a.train_frames, 1)
     model.set_training(False)
     results = {}
-    for name, s in (("plain", plain), ("clusters", clusters), ("learned", learned)):
+    runs = [("plain", plain), ("clusters", clusters), ("learned", learned)]
+    for m in [int(x) for x in a.sweep_candidates.split(",") if x.strip()]:
+        if m != a.candidates:
+            runs += [("%s_m%d" % (name, m), rl.copy_settings(st, candidate_count=m)) for name, st in runs[:3]]
+    for name, s in runs:
         mses = []
         for rep in range(4):
             rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=30_000_000 + 1000 * rep, frames=a.spp,
@@ -452,25 +460,37 @@ def run_equal_mse(a):
             if covered is not None:
                 d = d[covered]
             mses.append(float(d.mean()))
+        # Device time of the same a.spp-frame calls whose MSE was measured
+        # (per-call work, such as the logits and the cluster distributions,
+        # is shared by the call's frames).
         for _ in range(a.warmup):
-            rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=4, out_rgb=out, primitive=prim)
+            rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, out_rgb=out,
+                     primitive=prim)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for i in range(a.steps):
-            rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=40_000_000 + 4 * i, frames=4, out_rgb=out,
-                     primitive=prim)
+            rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=40_000_000 + a.spp * i, frames=a.spp,
+                     out_rgb=out, primitive=prim)
         e1.record()
         torch.cuda.synchronize()
-        results[name] = {"mse_at_spp": statistics.mean(mses), "ms_per_frame": e0.elapsed_time(e1) / (4 * a.steps)}
+        results[name] = {"mse_at_spp": statistics.mean(mses), "ms_per_frame": e0.elapsed_time(e1) / (a.spp * a.steps),
+                         "candidates": int(s.candidate_count)}
     ctx.check()
     base = results["plain"]
     for r in results.values():
         r["ms_to_plain_mse"] = r["ms_per_frame"] * a.spp * r["mse_at_spp"] / base["mse_at_spp"]
+    # Each method at its best candidate count (of those measured).
+    best = {}
+    for method in ("plain", "clusters", "learned"):
+        keys = [k for k in results if k == method or k.startswith(method + "_m")]
+        k = min(keys, key=lambda k: results[k]["ms_to_plain_mse"])
+        best[method] = {"run": k, "candidates": results[k]["candidates"],
+                        "ms_to_plain_mse": results[k]["ms_to_plain_mse"]}
     line = {
         "metric": "ms/frame to equal MSE, learned-proposal vs plain RIS (%dx%d, %d lights); Gsamples/s"
                   % (hs.width, hs.height, hs.light_count),
-        "value": results["learned"]["ms_to_plain_mse"], "unit": "ms", "higher_is_better": False,
+        "value": best["learned"]["ms_to_plain_mse"], "unit": "ms", "higher_is_better": False,
         "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "dtype": "f32 (MLP bf16/fp32)", "data": "synthetic",
         "config": {"workload": "equal MSE: %dx%d fBm heightfield, %d polygon lights (3-8 vertices) in %d k-means "
                                "clusters, %dk occluder triangles, M=%d, MSE at %d spp against a %d-spp FP64 plain-RIS "
@@ -480,6 +500,9 @@ def run_equal_mse(a):
                    "shadowed_target": a.shadowed_target},
         "plain_ms_to_equal_mse": base["ms_to_plain_mse"],
         "speedup_vs_plain": base["ms_to_plain_mse"] / results["learned"]["ms_to_plain_mse"],
+        "best_candidate_count": best,
+        "speedup_best_vs_plain": base["ms_to_plain_mse"] / best["learned"]["ms_to_plain_mse"],
+        "speedup_best_vs_best_plain": best["plain"]["ms_to_plain_mse"] / best["learned"]["ms_to_plain_mse"],
         "methods": results,
         "gsamples_per_s": {k: hs.pixels / (v["ms_per_frame"] / 1e3) / 1e9 for k, v in results.items()},
     }

@@ -89,6 +89,8 @@ struct risltc_scene_s {
 	// Cluster structure of the lights (risltc_scene_set_clusters).
 	risltc::ClusterView clusters;
 	void* d_cluster_offsets;
+	void* d_cluster_spans;
+	void* d_cluster_lane;  // lane-major bounds, power and sizes (ClusterView::*_lane)
 	void* d_light_cluster;
 	void* d_cluster_bounds;
 	void* d_cluster_power;
@@ -404,6 +406,8 @@ EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene) {
 	cudaFree(scene->d_pairs);
 	cudaFree(scene->d_triangles);
 	cudaFree(scene->d_cluster_offsets);
+	cudaFree(scene->d_cluster_spans);
+	cudaFree(scene->d_cluster_lane);
 	cudaFree(scene->d_light_cluster);
 	cudaFree(scene->d_cluster_bounds);
 	cudaFree(scene->d_cluster_power);
@@ -440,13 +444,35 @@ EXTERN_C int risltc_scene_set_clusters(risltc_scene_t* scene, const uint32_t* of
 	int st = risltc_cluster_summaries(std140.data(), n, maxv, offsets, cluster_count, bounds.data(), power.data());
 	if (st) return st;
 	std::vector<uint32_t> light_cluster(n);
-	for (uint32_t c = 0; c != cluster_count; ++c)
+	std::vector<uint32_t> spans(2 * (size_t) cluster_count);
+	for (uint32_t c = 0; c != cluster_count; ++c) {
+		spans[2 * c] = offsets[c];
+		spans[2 * c + 1] = offsets[c + 1] - offsets[c];
 		for (uint32_t l = offsets[c]; l != offsets[c + 1]; ++l) light_cluster[l] = c;
+	}
+	// Lane-major copies: slot j * 32 + l holds cluster l * per_lane + j.
+	const uint32_t per_lane = (cluster_count + 31) / 32, slots = 32 * per_lane;
+	std::vector<float> lane_data(4 * (size_t) slots + 2 * (size_t) slots, 0.0f);
+	float* bounds_lane = lane_data.data();
+	float* power_lane = bounds_lane + 4 * (size_t) slots;
+	uint32_t* size_lane = reinterpret_cast<uint32_t*>(power_lane + slots);
+	for (uint32_t l = 0; l != 32; ++l) {
+		for (uint32_t j = 0; j != per_lane; ++j) {
+			const uint32_t c = l * per_lane + j, t = j * 32 + l;
+			if (c >= cluster_count) continue;
+			for (int a = 0; a != 4; ++a) bounds_lane[4 * (size_t) t + a] = bounds[4 * (size_t) c + a];
+			power_lane[t] = power[c];
+			size_lane[t] = offsets[c + 1] - offsets[c];
+		}
+	}
 	cudaFree(scene->d_cluster_offsets);
+	cudaFree(scene->d_cluster_spans);
+	cudaFree(scene->d_cluster_lane);
 	cudaFree(scene->d_light_cluster);
 	cudaFree(scene->d_cluster_bounds);
 	cudaFree(scene->d_cluster_power);
-	scene->d_cluster_offsets = scene->d_light_cluster = scene->d_cluster_bounds = scene->d_cluster_power = nullptr;
+	scene->d_cluster_offsets = scene->d_cluster_spans = scene->d_cluster_lane = scene->d_light_cluster =
+	    scene->d_cluster_bounds = scene->d_cluster_power = nullptr;
 	scene->clusters = risltc::ClusterView{};
 	auto upload = [&](void** dst, const void* src, size_t bytes) {
 		if (e != cudaSuccess) return;
@@ -454,11 +480,17 @@ EXTERN_C int risltc_scene_set_clusters(risltc_scene_t* scene, const uint32_t* of
 		if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
 	};
 	upload(&scene->d_cluster_offsets, offsets, sizeof(uint32_t) * (cluster_count + 1));
+	upload(&scene->d_cluster_spans, spans.data(), sizeof(uint32_t) * spans.size());
+	upload(&scene->d_cluster_lane, lane_data.data(), sizeof(float) * lane_data.size());
 	upload(&scene->d_light_cluster, light_cluster.data(), sizeof(uint32_t) * n);
 	upload(&scene->d_cluster_bounds, bounds.data(), sizeof(float) * bounds.size());
 	upload(&scene->d_cluster_power, power.data(), sizeof(float) * power.size());
 	if (e != cudaSuccess) return cuda_status(e);
 	scene->clusters.offsets = (const uint32_t*) scene->d_cluster_offsets;
+	scene->clusters.spans = (const uint2*) scene->d_cluster_spans;
+	scene->clusters.bounds_lane = (const float4*) scene->d_cluster_lane;
+	scene->clusters.power_lane = (const float*) scene->d_cluster_lane + 4 * (size_t) slots;
+	scene->clusters.size_lane = (const uint32_t*) scene->d_cluster_lane + 5 * (size_t) slots;
 	scene->clusters.light_cluster = (const uint32_t*) scene->d_light_cluster;
 	scene->clusters.bounds = (const float4*) scene->d_cluster_bounds;
 	scene->clusters.power = (const float*) scene->d_cluster_power;

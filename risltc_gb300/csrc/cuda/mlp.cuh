@@ -4,7 +4,8 @@
 //   inputs (10): position (centred and scaled by the model's input
 //     transform), normal, outgoing direction, roughness;
 //   encoding (144): per input u: u, sin(2^k pi u), cos(2^k pi u), k = 0..5
-//     (130 features, zero-padded to 144);
+//     (130 features, zero-padded to 144), the higher frequencies from
+//     sincospi(u) by the double-angle formulas;
 //   layer 1: 144 -> 64, ReLU; layer 2: 64 -> 64, ReLU; layer 3: 64 -> K.
 //
 // Weights are BF16 (each layer stored [out][in]), biases FP32; products
@@ -23,7 +24,7 @@ constexpr int kMlpInputs = 10;
 constexpr int kMlpFrequencies = 6;
 constexpr int kMlpFeatures = 144;  // 10 * 13 = 130, padded to a multiple of 16
 constexpr int kMlpHidden = 64;
-constexpr int kMlpWarps = 4;
+constexpr int kMlpWarps = 8;
 
 // Offsets (in floats) of the parameters in the model's FP32 parameter vector.
 struct MlpLayout {
@@ -52,26 +53,31 @@ struct MlpParams {
 	__nv_bfloat16* logits;         // [pixel][k_count]
 };
 
-// The 10 raw inputs of pixel i.
-RL_DEV void mlp_inputs(const float* g, uint32_t np, uint32_t i, const float center[3], float inv_half_extent,
-                       float u[kMlpInputs]) {
+// Input `input` (0..9) of pixel i: position (centred and scaled), normal,
+// outgoing direction, roughness.
+RL_DEV float mlp_input(const float* g, uint32_t np, uint32_t i, const float center[3], float inv_half_extent,
+                       int input) {
 	const size_t snp = np;
-	for (int a = 0; a != 3; ++a) u[a] = (g[a * snp + i] - center[a]) * inv_half_extent;
-	for (int a = 0; a != 3; ++a) u[3 + a] = g[(3 + a) * snp + i];
-	for (int a = 0; a != 3; ++a) u[6 + a] = g[(6 + a) * snp + i];
-	u[9] = g[16 * snp + i];
+	if (input < 3) return (g[input * snp + i] - center[input]) * inv_half_extent;
+	return g[(input < 9 ? input : 16) * snp + i];
 }
 
-// Feature f of the encoding of the inputs u.
-RL_DEV float mlp_feature(const float u[kMlpInputs], int f) {
-	if (f >= kMlpInputs * 13) return 0.0f;
-	const int input = f / 13, kind = f % 13;
-	const float x = u[input];
-	if (kind == 0) return x;
-	const int k = (kind - 1) % kMlpFrequencies;
+// The 13 features of one input x: x, sin(2^k pi x) for k = 0..5, then
+// cos(2^k pi x) for k = 0..5.  sincospi once, then the double-angle
+// formulas (sin 2a = 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a));
+// their FP32 error stays far below the BF16 rounding of the features.
+RL_DEV void mlp_encode(float x, float out[13]) {
+	out[0] = x;
 	float s, c;
-	sincospif(x * (float) (1 << k), &s, &c);
-	return kind <= kMlpFrequencies ? s : c;
+	sincospif(x, &s, &c);
+#pragma unroll
+	for (int k = 0; k != kMlpFrequencies; ++k) {
+		out[1 + k] = s;
+		out[1 + kMlpFrequencies + k] = c;
+		const float s2 = 2.0f * s * c, c2 = (c - s) * (c + s);
+		s = s2;
+		c = c2;
+	}
 }
 
 RL_DEV uint32_t pack_bf16x2(float lo, float hi) {
@@ -161,13 +167,11 @@ static __global__ void __launch_bounds__(32 * kMlpWarps) mlp_logits_kernel(MlpPa
 		for (int idx = (int) lane; idx < 16 * kMlpInputs; idx += 32) {
 			const int r = idx / kMlpInputs, input = idx % kMlpInputs;
 			const uint32_t i = p0 + (uint32_t) r;
-			float u[kMlpInputs];
-			if (i < np)
-				mlp_inputs(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, u);
-			else
-				for (int a = 0; a != kMlpInputs; ++a) u[a] = 0.0f;
+			float e[13];
+			mlp_encode(i < np ? mlp_input(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, input) : 0.0f, e);
+#pragma unroll
 			for (int kind = 0; kind != 13; ++kind)
-				feat[r * kMlpFeatures + input * 13 + kind] = __float2bfloat16_rn(i < np ? mlp_feature(u, input * 13 + kind) : 0.0f);
+				feat[r * kMlpFeatures + input * 13 + kind] = __float2bfloat16_rn(i < np ? e[kind] : 0.0f);
 		}
 		for (int idx = (int) lane; idx < 16 * (kMlpFeatures - 130); idx += 32)
 			feat[(idx / (kMlpFeatures - 130)) * kMlpFeatures + 130 + idx % (kMlpFeatures - 130)] = __float2bfloat16_rn(0.0f);
@@ -292,10 +296,10 @@ static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrai
 			const int r = idx / kMlpFeatures, f = idx % kMlpFeatures;
 			const uint32_t j = base + r, i = pr.phase + j * pr.stride;
 			float v = 0.0f;
-			if (j < n_train) {
-				float u[kMlpInputs];
-				mlp_inputs(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, u);
-				v = mlp_feature(u, f);
+			if (j < n_train && f < kMlpInputs * 13) {
+				float e[13];
+				mlp_encode(mlp_input(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, f / 13), e);
+				v = e[f % 13];
 			}
 			feat[idx] = v;
 		}
