@@ -146,7 +146,8 @@ enum risltc_status_e {
 	RISLTC_ERROR_OUT_OF_MEMORY = 7,
 	RISLTC_ERROR_IO = 8,
 	RISLTC_ERROR_UNSUPPORTED = 9,
-	RISLTC_ERROR_TOO_LARGE = 10
+	RISLTC_ERROR_TOO_LARGE = 10,
+	RISLTC_ERROR_DEVICE_TIMEOUT = 11 /* a bounded device-side wait ran out (reported by risltc_ctx_check) */
 };
 
 /* Largest light vertex count (MAX_POLYGONAL_LIGHT_VERTEX_COUNT of

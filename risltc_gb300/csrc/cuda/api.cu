@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include "gbuffer.cuh"
 #include "mlp.cuh"
+#include "mlp_tc.cuh"
 #include "ris_binned.cuh"
 #include "ris_wavefront.cuh"
 
@@ -643,18 +644,20 @@ cudaError_t launch_logits(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_m
 	for (int a = 0; a != 3; ++a) q.center[a] = m->center[a];
 	q.inv_half_extent = m->inv_half_extent;
 	q.logits = logits;
-	const size_t smem = risltc::mlp_smem_bytes(m->cluster_count);
+	q.error = ctx->d_error;
 	static std::atomic<uint64_t> configured{0};
 	const uint64_t bit = 1ull << (ctx->device & 63);
 	if (!(configured.load() & bit)) {
-		cudaError_t e = cudaFuncSetAttribute(risltc::mlp_logits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                     (int) risltc::mlp_smem_bytes(risltc::kMaxClusters));
+		cudaError_t e = cudaFuncSetAttribute(risltc::mlp_logits_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                                     (int) risltc::mlp_tc_smem_bytes(risltc::kMaxClusters));
 		if (e != cudaSuccess) return e;
 		configured.fetch_or(bit);
 	}
-	const size_t tiles = ((size_t) gbuffer->width * gbuffer->height + 15) / 16;
-	const int grid = (int) std::min<size_t>((tiles + risltc::kMlpWarps - 1) / risltc::kMlpWarps, (size_t) ctx->sm_count * 2);
-	risltc::mlp_logits_kernel<<<grid, 32 * risltc::kMlpWarps, smem, stream>>>(q);
+	// At most two CTAs per SM fit in shared memory, so the two 256-column
+	// tensor-memory allocations of an SM never wait for each other.
+	const size_t tiles = ((size_t) gbuffer->width * gbuffer->height + risltc::kTcRows - 1) / risltc::kTcRows;
+	const int grid = (int) std::min<size_t>(tiles, (size_t) ctx->sm_count * 2);
+	risltc::mlp_logits_tc_kernel<<<grid, risltc::kTcThreads, risltc::mlp_tc_smem_bytes(m->cluster_count), stream>>>(q);
 	return cudaGetLastError();
 }
 
@@ -1176,6 +1179,7 @@ EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx) {
 		cudaMemsetAsync(ctx->d_error, 0, sizeof(uint32_t), ctx->stream);
 		cudaStreamSynchronize(ctx->stream);
 		if (bits & risltc::kErrorTraversalLimit) return RISLTC_ERROR_TRAVERSAL_LIMIT;
+		if (bits & risltc::kErrorTensorWait) return RISLTC_ERROR_DEVICE_TIMEOUT;
 		return RISLTC_ERROR_VERTEX_COUNT;
 	}
 	return RISLTC_OK;
@@ -1193,6 +1197,7 @@ EXTERN_C const char* risltc_status_string(int status) {
 	case RISLTC_ERROR_OUT_OF_MEMORY: return "out of memory";
 	case RISLTC_ERROR_IO: return "file could not be read";
 	case RISLTC_ERROR_UNSUPPORTED: return "unsupported setting";
+	case RISLTC_ERROR_DEVICE_TIMEOUT: return "a device-side wait exceeded its limit";
 	case RISLTC_ERROR_TOO_LARGE: return "frame larger than the static scratch of risltc_shade_noalloc";
 	default: return "unknown status";
 	}

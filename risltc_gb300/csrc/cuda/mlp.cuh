@@ -8,11 +8,9 @@
 //     sincospi(u) by the double-angle formulas;
 //   layer 1: 144 -> 64, ReLU; layer 2: 64 -> 64, ReLU; layer 3: 64 -> K.
 //
-// Weights are BF16 (each layer stored [out][in]), biases FP32; products
-// accumulate in FP32 on the tensor cores (mma.sync m16n8k16 BF16, one warp
-// per 16 pixels).  A layer's FP32 accumulator fragments are exactly the A
-// fragments of the next layer's product once biased, clamped and rounded to
-// BF16, so the hidden activations never leave the registers.
+// Weights are BF16 for inference (each layer stored [out][in]), biases FP32.
+// The forward pass runs on the tcgen05 tensor cores (mlp_tc.cuh); online
+// training (below) runs in FP32 on the CUDA cores.
 #pragma once
 #include <cuda_bf16.h>
 #include "proposal.cuh"
@@ -24,7 +22,6 @@ constexpr int kMlpInputs = 10;
 constexpr int kMlpFrequencies = 6;
 constexpr int kMlpFeatures = 144;  // 10 * 13 = 130, padded to a multiple of 16
 constexpr int kMlpHidden = 64;
-constexpr int kMlpWarps = 8;
 
 // Offsets (in floats) of the parameters in the model's FP32 parameter vector.
 struct MlpLayout {
@@ -51,6 +48,7 @@ struct MlpParams {
 	int k_count;                   // clusters, a multiple of 8
 	float center[3], inv_half_extent;
 	__nv_bfloat16* logits;         // [pixel][k_count]
+	uint32_t* error;               // the context's error word
 };
 
 // Input `input` (0..9) of pixel i: position (centred and scaled), normal,
@@ -83,135 +81,6 @@ RL_DEV void mlp_encode(float x, float out[13]) {
 RL_DEV uint32_t pack_bf16x2(float lo, float hi) {
 	const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
 	return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-// D = A * B + C for one m16n8k16 tile (A row-major 16x16, B col-major 16x8,
-// BF16; C and D FP32).
-RL_DEV void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1) {
-	asm volatile(
-	    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-	    "{%0,%1,%2,%3};\n"
-	    : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-	    : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// One hidden layer on A fragments held in registers: out = ReLU(W a + b) as
-// the next layer's A fragments.  a[kt][4]: kt = 16-column tiles of the input;
-// w: [64][in] BF16 in shared memory; b: 64 FP32.
-template <int KT>
-RL_DEV void mlp_hidden(const uint32_t (&a)[KT][4], const __nv_bfloat16* w, const float* b, uint32_t (&out)[4][4],
-                       uint32_t lane) {
-	const uint32_t g = lane / 4, t = lane % 4;
-	float acc[8][4];
-#pragma unroll
-	for (int nt = 0; nt != 8; ++nt) {
-		const float b0 = b[nt * 8 + 2 * t], b1 = b[nt * 8 + 2 * t + 1];
-		acc[nt][0] = b0;
-		acc[nt][1] = b1;
-		acc[nt][2] = b0;
-		acc[nt][3] = b1;
-	}
-#pragma unroll
-	for (int kt = 0; kt != KT; ++kt) {
-#pragma unroll
-		for (int nt = 0; nt != 8; ++nt) {
-			const __nv_bfloat16* row = w + (nt * 8 + g) * (KT * 16) + kt * 16 + 2 * t;
-			const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
-			const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
-			mma_bf16(acc[nt], a[kt][0], a[kt][1], a[kt][2], a[kt][3], b0, b1);
-		}
-	}
-#pragma unroll
-	for (int kt = 0; kt != 4; ++kt) {
-		out[kt][0] = pack_bf16x2(fmaxf(acc[2 * kt][0], 0.0f), fmaxf(acc[2 * kt][1], 0.0f));
-		out[kt][1] = pack_bf16x2(fmaxf(acc[2 * kt][2], 0.0f), fmaxf(acc[2 * kt][3], 0.0f));
-		out[kt][2] = pack_bf16x2(fmaxf(acc[2 * kt + 1][0], 0.0f), fmaxf(acc[2 * kt + 1][1], 0.0f));
-		out[kt][3] = pack_bf16x2(fmaxf(acc[2 * kt + 1][2], 0.0f), fmaxf(acc[2 * kt + 1][3], 0.0f));
-	}
-}
-
-// Shared memory: the three weight matrices (BF16), the three biases (FP32)
-// and per warp the encoded features of its 16 pixels (BF16).
-inline size_t mlp_smem_bytes(int k_count) {
-	return sizeof(__nv_bfloat16) * (kMlpHidden * kMlpFeatures + kMlpHidden * kMlpHidden + k_count * kMlpHidden) +
-	       sizeof(float) * (2 * kMlpHidden + k_count) + sizeof(__nv_bfloat16) * kMlpWarps * 16 * kMlpFeatures;
-}
-
-static __global__ void __launch_bounds__(32 * kMlpWarps) mlp_logits_kernel(MlpParams pr) {
-	extern __shared__ __align__(16) unsigned char mlp_smem[];
-	const int k_count = pr.k_count;
-	const MlpLayout lay = mlp_layout(k_count);
-	__nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(mlp_smem);
-	__nv_bfloat16* w2 = w1 + kMlpHidden * kMlpFeatures;
-	__nv_bfloat16* w3 = w2 + kMlpHidden * kMlpHidden;
-	float* b1 = reinterpret_cast<float*>(w3 + k_count * kMlpHidden);
-	float* b2 = b1 + kMlpHidden;
-	float* b3 = b2 + kMlpHidden;
-	__nv_bfloat16* feat = reinterpret_cast<__nv_bfloat16*>(b3 + k_count) + (threadIdx.x / 32) * 16 * kMlpFeatures;
-	// Stage the weights and biases once per block.
-	for (int j = threadIdx.x; j < kMlpHidden * kMlpFeatures; j += blockDim.x) w1[j] = pr.weights[lay.w1 + j];
-	for (int j = threadIdx.x; j < kMlpHidden * kMlpHidden; j += blockDim.x) w2[j] = pr.weights[lay.w2 + j];
-	for (int j = threadIdx.x; j < k_count * kMlpHidden; j += blockDim.x) w3[j] = pr.weights[lay.w3 + j];
-	for (int j = threadIdx.x; j < kMlpHidden; j += blockDim.x) {
-		b1[j] = pr.params[lay.b1 + j];
-		b2[j] = pr.params[lay.b2 + j];
-	}
-	for (int j = threadIdx.x; j < k_count; j += blockDim.x) b3[j] = pr.params[lay.b3 + j];
-	__syncthreads();
-	const uint32_t lane = threadIdx.x % 32, g = lane / 4, t = lane % 4;
-	const uint32_t np = pr.width * pr.height;
-	const uint32_t tiles = (np + 15) / 16;
-	for (uint32_t tile = blockIdx.x * kMlpWarps + threadIdx.x / 32; tile < tiles; tile += gridDim.x * kMlpWarps) {
-		const uint32_t p0 = tile * 16;
-		// Encode: lane handles (pixel, input) pairs; 13 features each.
-		for (int idx = (int) lane; idx < 16 * kMlpInputs; idx += 32) {
-			const int r = idx / kMlpInputs, input = idx % kMlpInputs;
-			const uint32_t i = p0 + (uint32_t) r;
-			float e[13];
-			mlp_encode(i < np ? mlp_input(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, input) : 0.0f, e);
-#pragma unroll
-			for (int kind = 0; kind != 13; ++kind)
-				feat[r * kMlpFeatures + input * 13 + kind] = __float2bfloat16_rn(i < np ? e[kind] : 0.0f);
-		}
-		for (int idx = (int) lane; idx < 16 * (kMlpFeatures - 130); idx += 32)
-			feat[(idx / (kMlpFeatures - 130)) * kMlpFeatures + 130 + idx % (kMlpFeatures - 130)] = __float2bfloat16_rn(0.0f);
-		__syncwarp();
-		// Layer 1 A fragments from shared memory.
-		uint32_t a1[kMlpFeatures / 16][4];
-#pragma unroll
-		for (int kt = 0; kt != kMlpFeatures / 16; ++kt) {
-			const __nv_bfloat16* r0 = feat + g * kMlpFeatures + kt * 16 + 2 * t;
-			const __nv_bfloat16* r8 = r0 + 8 * kMlpFeatures;
-			a1[kt][0] = *reinterpret_cast<const uint32_t*>(r0);
-			a1[kt][1] = *reinterpret_cast<const uint32_t*>(r8);
-			a1[kt][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
-			a1[kt][3] = *reinterpret_cast<const uint32_t*>(r8 + 8);
-		}
-		__syncwarp();
-		uint32_t h1[4][4], h2[4][4];
-		mlp_hidden<kMlpFeatures / 16>(a1, w1, b1, h1, lane);
-		mlp_hidden<4>(h1, w2, b2, h2, lane);
-		// Layer 3, eight clusters at a time, written as BF16 logits.
-		const uint32_t row0 = p0 + g, row8 = p0 + g + 8;
-		for (int nt = 0; nt < k_count / 8; ++nt) {
-			float acc[4];
-			const float c0 = b3[nt * 8 + 2 * t], c1 = b3[nt * 8 + 2 * t + 1];
-			acc[0] = c0;
-			acc[1] = c1;
-			acc[2] = c0;
-			acc[3] = c1;
-#pragma unroll
-			for (int kt = 0; kt != 4; ++kt) {
-				const __nv_bfloat16* row = w3 + (nt * 8 + g) * kMlpHidden + kt * 16 + 2 * t;
-				mma_bf16(acc, h2[kt][0], h2[kt][1], h2[kt][2], h2[kt][3], *reinterpret_cast<const uint32_t*>(row),
-				         *reinterpret_cast<const uint32_t*>(row + 8));
-			}
-			if (row0 < np)
-				*reinterpret_cast<uint32_t*>(pr.logits + (size_t) row0 * k_count + nt * 8 + 2 * t) = pack_bf16x2(acc[0], acc[1]);
-			if (row8 < np)
-				*reinterpret_cast<uint32_t*>(pr.logits + (size_t) row8 * k_count + nt * 8 + 2 * t) = pack_bf16x2(acc[2], acc[3]);
-		}
-	}
 }
 
 // FP32 parameters to their BF16 copy.

@@ -54,12 +54,17 @@ def test_parameter_count():
 
 
 @pytest.mark.gpu
-def test_model_logits_match_numpy(gpu):
+@pytest.mark.parametrize("k", [64, 72, 256])
+def test_model_logits_match_numpy(gpu, k):
+    """The tcgen05 forward pass (128-pixel tiles, clusters padded to a
+    multiple of 16 and produced 128 at a time) against NumPy, on a frame
+    whose pixel count is not a multiple of 128."""
     import torch
     import risltc_gb300 as rl
     sc = gd.scene("hf")
+    assert (sc["width"] * sc["height"]) % 128 != 0
     ctx = rl.Context(0)
-    model = rl.Model(ctx, 64, seed=7)
+    model = rl.Model(ctx, k, seed=7)
     rng = np.random.default_rng(1)
     params = model.get_params()
     # Larger output weights and non-zero biases than the initialisation.
@@ -73,7 +78,7 @@ def test_model_logits_match_numpy(gpu):
     ctx.check()
     model.close()
     ctx.close()
-    want = reference_logits(params, 64, encode(sc["gbuffer"], center, half))
+    want = reference_logits(params, k, encode(sc["gbuffer"], center, half))
     err = np.abs(got - want)
     scale = np.abs(want).max()
     assert np.quantile(err, 0.999) <= 0.02 * scale
