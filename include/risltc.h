@@ -552,6 +552,15 @@ EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, 
 /* Synchronises the context's stream and returns the first error recorded by
    a kernel since the last check (RISLTC_OK if none). */
 EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx);
+
+/* Fault injection for tests of the failure paths, made on the host: with
+   RISLTC_FAULT_TENSOR_WAIT the next learned-proposal logits launch issues no
+   tensor-core products, so its bounded waits (one second each) run out, the
+   kernel records the timeout, frees its tensor memory and returns, and the
+   next risltc_ctx_check reports RISLTC_ERROR_DEVICE_TIMEOUT; the context stays
+   usable.  Nothing faults, traps or hangs. */
+#define RISLTC_FAULT_TENSOR_WAIT 1u
+EXTERN_C int risltc_ctx_inject_fault(risltc_ctx_t* ctx, uint32_t faults);
 EXTERN_C const char* risltc_status_string(int status);
 
 #endif /* RISLTC_H */

@@ -89,6 +89,11 @@ class Context:
     def check(self):
         check(self._lib.risltc_ctx_check(self._h), "risltc_ctx_check")
 
+    def inject_fault(self, tensor_wait=False):
+        """risltc_ctx_inject_fault: host-made faults for tests of the failure
+        paths (see include/risltc.h)."""
+        check(self._lib.risltc_ctx_inject_fault(self._h, 1 if tensor_wait else 0), "risltc_ctx_inject_fault")
+
     def profile(self, enable=True):
         """Per-kernel CUDA-event times (ms) of the shading calls since the last
         call, then switches timing on or off.  Returns a dict: candidates

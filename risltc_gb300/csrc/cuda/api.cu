@@ -72,6 +72,9 @@ struct risltc_ctx_s {
 	int batch_streams_created;
 	// Kernel timing: five events per shading call (before, between and after
 	// the phases), up to 64 calls between queries.
+	// Fault injection (risltc_ctx_inject_fault): RISLTC_FAULT_* bits, each
+	// consumed by the next launch it applies to.
+	uint32_t inject;
 	int profiling;
 	int timed_calls;
 	cudaEvent_t events[64][5];
@@ -645,6 +648,8 @@ cudaError_t launch_logits(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_m
 	q.inv_half_extent = m->inv_half_extent;
 	q.logits = logits;
 	q.error = ctx->d_error;
+	q.skip_issue = (ctx->inject & RISLTC_FAULT_TENSOR_WAIT) ? 1u : 0u;
+	ctx->inject &= ~(uint32_t) RISLTC_FAULT_TENSOR_WAIT;
 	static std::atomic<uint64_t> configured{0};
 	const uint64_t bit = 1ull << (ctx->device & 63);
 	if (!(configured.load() & bit)) {
@@ -1166,6 +1171,12 @@ EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, 
 	ctx->timed_calls = 0;
 	ctx->profiling = enable;
 	return status;
+}
+
+EXTERN_C int risltc_ctx_inject_fault(risltc_ctx_t* ctx, uint32_t faults) {
+	if (!ctx || (faults & ~(uint32_t) RISLTC_FAULT_TENSOR_WAIT)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	ctx->inject |= faults;
+	return RISLTC_OK;
 }
 
 EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx) {

@@ -49,6 +49,7 @@ struct MlpParams {
 	float center[3], inv_half_extent;
 	__nv_bfloat16* logits;         // [pixel][k_count]
 	uint32_t* error;               // the context's error word
+	uint32_t skip_issue;           // fault injection: issue no tensor-core products
 };
 
 // Input `input` (0..9) of pixel i: position (centred and scaled), normal,

@@ -24,7 +24,7 @@ constexpr int kTcRows = 128;      // pixels per tile: M of every product
 constexpr int kTcThreads = 128;   // warp w reads tensor-memory lanes 32w .. 32w + 31
 constexpr uint32_t kTcColumns = 256;
 constexpr int kTcChunk = 128;     // clusters per layer-3 product (N)
-constexpr uint32_t kTcWaitLimit = 1u << 22;
+constexpr uint64_t kTcWaitNs = 1000000000ull;  // a tensor-core wait gives up after one second
 constexpr uint32_t kErrorTensorWait = 1u << 2;  // error-word bit: a tensor-core wait ran out
 
 RL_DEV uint32_t smem_address(const void* p) { return (uint32_t) __cvta_generic_to_shared(p); }
@@ -78,10 +78,20 @@ RL_DEV bool mbarrier_try_wait(uint32_t bar, uint32_t parity) {
 	return done != 0;
 }
 
-// Waits for phase `parity` of the mbarrier, at most kTcWaitLimit polls.
+RL_DEV uint64_t global_ns() {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+	return t;
+}
+
+// Waits for phase `parity` of the mbarrier for at most kTcWaitNs (and at
+// most 2^28 polls).
 RL_DEV bool tc_wait(uint32_t bar, uint32_t parity) {
-	for (uint32_t i = 0; i != kTcWaitLimit; ++i)
+	const uint64_t t0 = global_ns();
+	for (uint32_t i = 0; i != (1u << 28); ++i) {
 		if (mbarrier_try_wait(bar, parity)) return true;
+		if ((i & 255u) == 255u && global_ns() - t0 > kTcWaitNs) return false;
+	}
 	return false;
 }
 
@@ -173,8 +183,10 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 	uint32_t parity = 0;
 	bool failed = false;
 	// One product group: issued by thread 0, then every thread waits for it.
+	// With pr.skip_issue (fault injection) nothing is issued or committed, so
+	// the wait runs out.
 	auto run = [&](auto issue) {
-		if (tid == 0) {
+		if (tid == 0 && !pr.skip_issue) {
 			issue();
 			tc_commit(bar);
 		}
@@ -282,7 +294,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 	}
 	if (failed) {
 		if (tid == 0) atomicOr(pr.error, kErrorTensorWait);
-		tc_wait(bar, parity ^ 1u);  // the product still in flight (its phase), bounded
+		if (!pr.skip_issue) tc_wait(bar, parity ^ 1u);  // the product still in flight (its phase), bounded
 	}
 	tc_fence_before();
 	__syncthreads();

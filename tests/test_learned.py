@@ -199,3 +199,29 @@ def test_online_training_moves_the_proposal_towards_the_targets(gpu):
     model.close()
     ctx.close()
     assert after < 0.5 * before
+
+
+@pytest.mark.gpu
+def test_tensor_wait_timeout_is_reported_and_the_context_survives(gpu):
+    """Fault injection on the host: the logits launch issues no tensor-core
+    products, its bounded waits run out after a second, the kernel records
+    the timeout and frees its tensor memory; risltc_ctx_check reports
+    RISLTC_ERROR_DEVICE_TIMEOUT and the next launch is correct."""
+    import torch
+    import risltc_gb300 as rl
+    sc = gd.scene("hf")
+    ctx = rl.Context(0)
+    model = rl.Model(ctx, 64, seed=3)
+    g = torch.from_numpy(np.ascontiguousarray(sc["gbuffer"])).cuda()
+    good = model.logits(g, sc["width"], sc["height"]).cpu().numpy()
+    ctx.check()
+    ctx.inject_fault(tensor_wait=True)
+    model.logits(g, sc["width"], sc["height"])
+    with pytest.raises(rl.RisltcError) as e:
+        ctx.check()
+    assert e.value.status == 11  # RISLTC_ERROR_DEVICE_TIMEOUT
+    again = model.logits(g, sc["width"], sc["height"]).cpu().numpy()
+    ctx.check()
+    assert np.array_equal(again, good)
+    model.close()
+    ctx.close()
