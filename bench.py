@@ -202,6 +202,10 @@ def cpu_sample(hs, a, seconds_target, threads=0, seed=1, count_ops=True, repeats
         out["candidate_flops_per_sample"] = per_candidate * a.candidates
         out["shade_flops_per_sample"] = lit["flops"] / m - per_candidate * a.candidates
         out["trace_flops_per_sample"] = (ops["flops"] - lit["flops"]) / m
+        # Traversal bytes of the same queries on the identical BVH: 32 bytes
+        # per box tested (the device reads a child pair's two boxes, 64 bytes,
+        # per inner node) and 48 per triangle tested.
+        out["trace_bytes_per_sample"] = (32.0 * ops["boxes"] + 48.0 * ops["triangles"]) / m
         out["ops"] = {k: v for k, v in ops.items() if k != "rgb"}
     return out
 
@@ -354,6 +358,15 @@ def run_ours(a, rank, world, local_rank):
         kernels["ris_candidates_binned_kernel"]["flops_per_sample"] = info["candidate_flops_per_sample"]
         kernels["ris_sample_kernel"]["flops_per_sample"] = info["shade_flops_per_sample"]
         kernels["shadow_trace_kernel"]["flops_per_sample"] = info["trace_flops_per_sample"]
+        tk = kernels["shadow_trace_kernel"]
+        tk["bytes_per_sample"] = info["trace_bytes_per_sample"]
+        tk["achieved_gbs"] = (tk["bytes_per_sample"] * samples_per_step / (tk["ms_per_launch"] / 1e3) / 1e9
+                              if tk["ms_per_launch"] > 0 else 0.0)
+        if peaks.get("hbm_gbs"):
+            # The BVH (about 14 MB) stays in L2/L1, so this is the node and
+            # triangle traffic the traversal moves, against HBM copy bandwidth
+            # for scale (ray sort included in the timed phase).
+            tk["gbs_frac_of_hbm"] = tk["achieved_gbs"] / peaks["hbm_gbs"]
         kernels["ris_resolve_kernel"]["flops_per_sample"] = 0.0
         for k in kernels.values():
             k["achieved_tflops"] = (k["flops_per_sample"] * samples_per_step / (k["ms_per_launch"] / 1e3) / 1e12

@@ -171,7 +171,8 @@ def render(scene, settings, gbuffer, width, height, random_number_x, primitive=N
 
 
 class OpCounts(ctypes.Structure):
-    _fields_ = [(k, ctypes.c_uint64) for k in ("add", "mul", "fma", "div", "sqrt", "atan", "sincos", "acos", "cmp")]
+    _fields_ = [(k, ctypes.c_uint64) for k in ("add", "mul", "fma", "div", "sqrt", "atan", "sincos", "acos", "cmp",
+                                               "boxes", "triangles")]
 
 
 # FP32 operations inside one call of each transcendental of include/risltc_math.h

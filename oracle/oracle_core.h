@@ -811,6 +811,12 @@ static int ray_triangle(vec3_t o, vec3_t d, const float* t, R t_min, R t_max) {
 	return tt >= t_min && tt <= t_max;
 }
 
+/* Traversal tallies of the op-counting build (no-ops elsewhere). */
+#ifndef ORACLE_COUNT_BOX
+#define ORACLE_COUNT_BOX() ((void) 0)
+#define ORACLE_COUNT_TRIANGLE() ((void) 0)
+#endif
+
 static int any_hit(const oracle_scene_t* s, vec3_t o, vec3_t d, R t_min, R t_max) {
 	if (s->triangle_count == 0) return 0;
 	if (!s->bvh_nodes) {
@@ -828,6 +834,7 @@ static int any_hit(const oracle_scene_t* s, vec3_t o, vec3_t d, R t_min, R t_max
 	stack[sp++] = 0;
 	while (sp) {
 		const float* n = s->bvh_nodes + 8 * (size_t) stack[--sp];
+		ORACLE_COUNT_BOX();
 		R lo = t_min, hi = t_max;
 		for (int a = 0; a != 3; ++a) {
 			R t0 = ((R) n[a] - org[a]) * inv_d[a];
@@ -845,8 +852,10 @@ static int any_hit(const oracle_scene_t* s, vec3_t o, vec3_t d, R t_min, R t_max
 			stack[sp++] = first + 1;
 			stack[sp++] = first;
 		} else {
-			for (int k = 0; k != count; ++k)
+			for (int k = 0; k != count; ++k) {
+				ORACLE_COUNT_TRIANGLE();
 				if (ray_triangle(o, d, s->triangles + 12 * (size_t) (first + k), t_min, t_max)) return 1;
+			}
 		}
 	}
 	return 0;

@@ -10,6 +10,7 @@
 
 struct OracleOpCounts {
 	uint64_t add, mul, fma, div, sqrt, atan, sincos, acos, cmp;
+	uint64_t boxes, triangles;  // BVH box tests and ray-triangle tests of the shadow queries
 };
 static OracleOpCounts g_ops;
 
@@ -62,6 +63,8 @@ static inline void cf_sincos(CF a, CF* s, CF* c) {
 #define R_ISINF(x) (std::isinf((x).v))
 #define R_INF CF(INFINITY)
 #define R_EXPONENT_FLIP(x) CF(rl_u2f(rl_f2u((x).v) ^ 0x7F800000u))
+#define ORACLE_COUNT_BOX() (++g_ops.boxes)
+#define ORACLE_COUNT_TRIANGLE() (++g_ops.triangles)
 #define ORACLE_SUFFIX _opcount_impl
 #define ORACLE_OUT_T float
 #include "oracle_core.h"
