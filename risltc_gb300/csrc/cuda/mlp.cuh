@@ -115,8 +115,16 @@ namespace risltc {
 // mixed by shadowed_weight.  Forward and backward run in FP32 from the FP32 master
 // parameters, one block per 32 training pixels, partial weight gradients
 // summed in shared memory and added to the gradient vector once per block.
-constexpr int kTrainPixels = 32;   // training pixels per block step
+// In the products lane l takes training pixel l and each warp a share of the
+// outputs, so every weight load is the same address across the warp (one
+// broadcast) and the activations are read from shared-memory rows whose odd
+// strides put the 32 pixels in 32 banks.
+constexpr int kTrainPixels = 32;   // training pixels per block step (one per lane)
 constexpr int kTrainThreads = 256;
+constexpr int kTrainWarps = kTrainThreads / 32;
+constexpr int kFeatStride = kMlpFeatures + 1;   // odd row strides in shared memory
+constexpr int kHiddenStride = kMlpHidden + 1;
+__host__ __device__ inline int train_logit_stride(int k_count) { return k_count | 1; }
 
 struct MlpTrainParams {
 	const float* gbuffer;
@@ -144,59 +152,58 @@ struct MlpTrainParams {
 };
 
 inline size_t mlp_train_smem_bytes(int k_count) {
-	return sizeof(float) * kTrainPixels * (kMlpFeatures + 4 * kMlpHidden + k_count);
+	return sizeof(float) * kTrainPixels * (kFeatStride + 4 * kHiddenStride + train_logit_stride(k_count));
 }
 
 static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrainParams pr) {
 	extern __shared__ __align__(16) float train_smem[];
 	const int k_count = pr.k_count;
 	const MlpLayout lay = mlp_layout(k_count);
-	float* feat = train_smem;                          // [32][144]
-	float* h1 = feat + kTrainPixels * kMlpFeatures;    // [32][64]
-	float* h2 = h1 + kTrainPixels * kMlpHidden;        // [32][64]
-	float* dz = h2 + kTrainPixels * kMlpHidden;        // [32][K] logits, then their gradient
-	float* d2 = dz + kTrainPixels * k_count;           // [32][64]
-	float* d1 = d2 + kTrainPixels * kMlpHidden;        // [32][64]
+	const int ks = train_logit_stride(k_count);
+	float* feat = train_smem;                          // [32][145]
+	float* h1 = feat + kTrainPixels * kFeatStride;     // [32][65]
+	float* h2 = h1 + kTrainPixels * kHiddenStride;     // [32][65]
+	float* dz = h2 + kTrainPixels * kHiddenStride;     // [32][ks] logits, then their gradient
+	float* d2 = dz + kTrainPixels * ks;                // [32][65]
+	float* d1 = d2 + kTrainPixels * kHiddenStride;     // [32][65]
 	const uint32_t np = pr.width * pr.height;
 	const uint32_t n_train = np > pr.phase ? (np - pr.phase + pr.stride - 1) / pr.stride : 0;
-	const int tid = threadIdx.x;
+	const int tid = threadIdx.x, px = tid % 32, warp = tid / 32;
 	for (uint32_t base = blockIdx.x * kTrainPixels; base < n_train; base += gridDim.x * kTrainPixels) {
 		// Encode the block's training pixels (invalid ones get zero weight).
-		for (int idx = tid; idx < kTrainPixels * kMlpFeatures; idx += kTrainThreads) {
-			const int r = idx / kMlpFeatures, f = idx % kMlpFeatures;
+		for (int idx = tid; idx < kTrainPixels * kMlpInputs; idx += kTrainThreads) {
+			const int r = idx / kMlpInputs, input = idx % kMlpInputs;
 			const uint32_t j = base + r, i = pr.phase + j * pr.stride;
-			float v = 0.0f;
-			if (j < n_train && f < kMlpInputs * 13) {
-				float e[13];
-				mlp_encode(mlp_input(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, f / 13), e);
-				v = e[f % 13];
-			}
-			feat[idx] = v;
+			float e[13];
+			mlp_encode(j < n_train ? mlp_input(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, input) : 0.0f, e);
+#pragma unroll
+			for (int kind = 0; kind != 13; ++kind) feat[r * kFeatStride + input * 13 + kind] = j < n_train ? e[kind] : 0.0f;
+		}
+		for (int idx = tid; idx < kTrainPixels * (kMlpFeatures - kMlpInputs * 13); idx += kTrainThreads) {
+			const int r = idx / (kMlpFeatures - kMlpInputs * 13), f = kMlpInputs * 13 + idx % (kMlpFeatures - kMlpInputs * 13);
+			feat[r * kFeatStride + f] = 0.0f;
 		}
 		__syncthreads();
-		// Forward: h1, h2 (ReLU), logits.
-		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
-			const int r = idx / kMlpHidden, o = idx % kMlpHidden;
+		// Forward: h1, h2 (ReLU), logits; lane = pixel, warps share the outputs.
+		for (int o = warp; o < kMlpHidden; o += kTrainWarps) {
 			float acc = pr.params[lay.b1 + o];
 			const float* w = pr.params + lay.w1 + o * kMlpFeatures;
-			for (int f = 0; f != kMlpFeatures; ++f) acc += w[f] * feat[r * kMlpFeatures + f];
-			h1[idx] = fmaxf(acc, 0.0f);
+			for (int f = 0; f != kMlpFeatures; ++f) acc += w[f] * feat[px * kFeatStride + f];
+			h1[px * kHiddenStride + o] = fmaxf(acc, 0.0f);
 		}
 		__syncthreads();
-		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
-			const int r = idx / kMlpHidden, o = idx % kMlpHidden;
+		for (int o = warp; o < kMlpHidden; o += kTrainWarps) {
 			float acc = pr.params[lay.b2 + o];
 			const float* w = pr.params + lay.w2 + o * kMlpHidden;
-			for (int f = 0; f != kMlpHidden; ++f) acc += w[f] * h1[r * kMlpHidden + f];
-			h2[idx] = fmaxf(acc, 0.0f);
+			for (int f = 0; f != kMlpHidden; ++f) acc += w[f] * h1[px * kHiddenStride + f];
+			h2[px * kHiddenStride + o] = fmaxf(acc, 0.0f);
 		}
 		__syncthreads();
-		for (int idx = tid; idx < kTrainPixels * k_count; idx += kTrainThreads) {
-			const int r = idx / k_count, o = idx % k_count;
+		for (int o = warp; o < k_count; o += kTrainWarps) {
 			float acc = pr.params[lay.b3 + o];
 			const float* w = pr.params + lay.w3 + o * kMlpHidden;
-			for (int f = 0; f != kMlpHidden; ++f) acc += w[f] * h2[r * kMlpHidden + f];
-			dz[idx] = acc;
+			for (int f = 0; f != kMlpHidden; ++f) acc += w[f] * h2[px * kHiddenStride + f];
+			dz[px * ks + o] = acc;
 		}
 		__syncthreads();
 		// Softmax and target per pixel: one warp per pixel.
@@ -204,7 +211,7 @@ static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrai
 			const int lane = tid % 32;
 			const uint32_t j = base + r, i = pr.phase + j * pr.stride;
 			const bool valid = j < n_train && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
-			float* z = dz + r * k_count;
+			float* z = dz + r * ks;
 			float m = -INFINITY;
 			for (int c = lane; c < k_count; c += 32) m = fmaxf(m, z[c]);
 			for (int d = 16; d != 0; d >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, d));
@@ -243,38 +250,40 @@ static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrai
 			__syncwarp();
 		}
 		__syncthreads();
-		// Backward: d2 = (W3^T dz) * [h2 > 0], d1 = (W2^T d2) * [h1 > 0].
-		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
-			const int r = idx / kMlpHidden, f = idx % kMlpHidden;
+		// Backward: d2 = (W3^T dz) * [h2 > 0], d1 = (W2^T d2) * [h1 > 0];
+		// lane = pixel, warps share the outputs.
+		for (int f = warp; f < kMlpHidden; f += kTrainWarps) {
 			float acc = 0.0f;
-			for (int o = 0; o != k_count; ++o) acc += pr.params[lay.w3 + o * kMlpHidden + f] * dz[r * k_count + o];
-			d2[idx] = h2[idx] > 0.0f ? acc : 0.0f;
+			for (int o = 0; o != k_count; ++o) acc += pr.params[lay.w3 + o * kMlpHidden + f] * dz[px * ks + o];
+			d2[px * kHiddenStride + f] = h2[px * kHiddenStride + f] > 0.0f ? acc : 0.0f;
 		}
 		__syncthreads();
-		for (int idx = tid; idx < kTrainPixels * kMlpHidden; idx += kTrainThreads) {
-			const int r = idx / kMlpHidden, f = idx % kMlpHidden;
+		for (int f = warp; f < kMlpHidden; f += kTrainWarps) {
 			float acc = 0.0f;
-			for (int o = 0; o != kMlpHidden; ++o) acc += pr.params[lay.w2 + o * kMlpHidden + f] * d2[r * kMlpHidden + o];
-			d1[idx] = h1[idx] > 0.0f ? acc : 0.0f;
+			for (int o = 0; o != kMlpHidden; ++o) acc += pr.params[lay.w2 + o * kMlpHidden + f] * d2[px * kHiddenStride + o];
+			d1[px * kHiddenStride + f] = h1[px * kHiddenStride + f] > 0.0f ? acc : 0.0f;
 		}
 		__syncthreads();
 		// Weight gradients summed over the block's pixels, added once.
 		for (int idx = tid; idx < k_count * (kMlpHidden + 1); idx += kTrainThreads) {
 			const int o = idx / (kMlpHidden + 1), f = idx % (kMlpHidden + 1);
 			float acc = 0.0f;
-			for (int r = 0; r != kTrainPixels; ++r) acc += dz[r * k_count + o] * (f < kMlpHidden ? h2[r * kMlpHidden + f] : 1.0f);
+			for (int r = 0; r != kTrainPixels; ++r)
+				acc += dz[r * ks + o] * (f < kMlpHidden ? h2[r * kHiddenStride + f] : 1.0f);
 			if (acc != 0.0f) atomicAdd(pr.grad + (f < kMlpHidden ? lay.w3 + o * kMlpHidden + f : lay.b3 + o), acc);
 		}
 		for (int idx = tid; idx < kMlpHidden * (kMlpHidden + 1); idx += kTrainThreads) {
 			const int o = idx / (kMlpHidden + 1), f = idx % (kMlpHidden + 1);
 			float acc = 0.0f;
-			for (int r = 0; r != kTrainPixels; ++r) acc += d2[r * kMlpHidden + o] * (f < kMlpHidden ? h1[r * kMlpHidden + f] : 1.0f);
+			for (int r = 0; r != kTrainPixels; ++r)
+				acc += d2[r * kHiddenStride + o] * (f < kMlpHidden ? h1[r * kHiddenStride + f] : 1.0f);
 			if (acc != 0.0f) atomicAdd(pr.grad + (f < kMlpHidden ? lay.w2 + o * kMlpHidden + f : lay.b2 + o), acc);
 		}
 		for (int idx = tid; idx < kMlpHidden * (kMlpFeatures + 1); idx += kTrainThreads) {
 			const int o = idx / (kMlpFeatures + 1), f = idx % (kMlpFeatures + 1);
 			float acc = 0.0f;
-			for (int r = 0; r != kTrainPixels; ++r) acc += d1[r * kMlpHidden + o] * (f < kMlpFeatures ? feat[r * kMlpFeatures + f] : 1.0f);
+			for (int r = 0; r != kTrainPixels; ++r)
+				acc += d1[r * kHiddenStride + o] * (f < kMlpFeatures ? feat[r * kFeatStride + f] : 1.0f);
 			if (acc != 0.0f) atomicAdd(pr.grad + (f < kMlpFeatures ? lay.w1 + o * kMlpFeatures + f : lay.b1 + o), acc);
 		}
 		__syncthreads();
