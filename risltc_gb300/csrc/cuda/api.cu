@@ -618,8 +618,10 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 		if (e != cudaSuccess) return e;
 		configured.fetch_or(bit);
 	}
+	// Two blocks per SM where their shared memory fits (up to about 500
+	// clusters), one otherwise.
 	const int blocks = (int) std::min<uint32_t>((n_train + risltc::kTrainPixels - 1) / risltc::kTrainPixels,
-	                                            (uint32_t) ctx->sm_count);
+	                                            (uint32_t) ctx->sm_count * 2);
 	risltc::mlp_train_kernel<<<blocks, risltc::kTrainThreads, risltc::mlp_train_smem_bytes(m->cluster_count), stream>>>(t);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
