@@ -1,0 +1,99 @@
+"""Edge cases of the shading path, through the C ABI, against the oracle.
+
+Frames that are all background, a single pixel, a single light, one
+candidate and the largest candidate count (4096) give the oracle's pixels
+bit for bit in exact numerics; arguments past the limits (4097 candidates,
+an empty frame) and non-finite occluders are rejected before any work.
+"""
+import numpy as np
+import pytest
+
+import golden_data as gd
+from test_gpu_parity import gpu_render, oracle_render
+
+pytestmark = pytest.mark.gpu
+
+RIS = dict(technique="ltc_cp", light_sampling="ris", mis="optimal_clamped", sample_count=1, light_samples=1,
+           fast_atan=False)
+
+
+@pytest.fixture(scope="module")
+def rl(gpu):
+    import torch
+    import risltc_gb300 as rl
+    ctx = rl.Context(0)
+    yield rl, ctx, torch
+    ctx.close()
+
+
+def heightfield(w, h, lights, tris, seed):
+    import risltc_gb300 as rlm
+    hs = rlm.scenes.heightfield(w, h, light_count=lights, triangle_count=tris, seed=seed, vertex_counts=(3, 8))
+    return dict(width=hs.width, height=hs.height, gbuffer=hs.gbuffer, primitive=hs.primitive, lights=hs.lights,
+                triangles=hs.triangles, max_vertex_count=hs.max_vertex_count)
+
+
+def rn_of(frame):
+    import risltc_gb300 as rlm
+    return rlm.noise_constants(frame)[0]
+
+
+def check_bit_exact(rl_tuple, sc, candidates, frame=3):
+    c = dict(RIS, candidates=candidates)
+    rgb, _, idx, wp = gpu_render(rl_tuple, sc, c, noise_seed=frame)
+    orgb, ores, _ = oracle_render(sc, c, rn_of(frame))
+    assert np.array_equal(rgb, orgb)
+    assert np.array_equal(idx, ores["light_index"])
+    assert np.array_equal(wp[:, 0], ores["w_sum"].astype(np.float32))
+    return rgb, idx
+
+
+def test_all_background_frame(rl):
+    sc = heightfield(40, 24, 64, 500, seed=4)
+    sc["primitive"] = np.full(sc["width"] * sc["height"], 0xFFFFFFFF, np.uint32)
+    rgb, idx = check_bit_exact(rl, sc, 16)
+    assert np.all(rgb == 0.0) and np.all(idx == -1)
+
+
+def test_single_pixel_frame(rl):
+    sc = heightfield(33, 17, 64, 500, seed=5)
+    covered = np.flatnonzero(sc["primitive"] == 0)[0]
+    sc["gbuffer"] = np.ascontiguousarray(sc["gbuffer"][:, covered:covered + 1])
+    sc["primitive"] = sc["primitive"][covered:covered + 1].copy()
+    sc["width"], sc["height"] = 1, 1
+    check_bit_exact(rl, sc, 32)
+
+
+def test_single_light(rl):
+    sc = heightfield(48, 27, 1, 800, seed=6)
+    rgb, idx = check_bit_exact(rl, sc, 8)
+    lit = idx >= 0
+    assert lit.any() and np.all(idx[lit] == 0)
+
+
+@pytest.mark.parametrize("candidates", [1, 4096])
+def test_candidate_count_limits(rl, candidates):
+    sc = heightfield(16, 8, 300, 800, seed=7)
+    check_bit_exact(rl, sc, candidates)
+
+
+def test_arguments_past_the_limits_are_rejected(rl):
+    rlm, ctx, torch = rl
+    sc = heightfield(16, 8, 16, 100, seed=8)
+    l0, l1, k = gd.ltc()
+    scene = rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    g = torch.from_numpy(sc["gbuffer"]).cuda()
+    out = torch.full((sc["width"] * sc["height"], 3), -1.0, device="cuda")
+    with pytest.raises(rlm.RisltcError):
+        rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(candidates=4097), out_rgb=out)
+    with pytest.raises(rlm.RisltcError):
+        rlm.shade(ctx, scene, g, 0, sc["height"], rlm.settings(), out_rgb=out)
+    with pytest.raises(rlm.RisltcError):
+        rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(), frames=0, out_rgb=out)
+    ctx.check()
+    assert torch.all(out == -1.0)  # nothing ran
+    scene.close()
+    bad = sc["triangles"].copy()
+    bad[3, 4] = np.nan
+    with pytest.raises(rlm.RisltcError):
+        rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, bad)
