@@ -47,12 +47,27 @@ struct ShadowRay {
 	float4 dir_tmax;
 };
 
+// Technique j's two contributions (unoccluded, occluded) into floats
+// 6j .. 6j + 5 of a sample record.
+RL_DEV void store_contributions(SampleRecord* dst, int j, f3 c0, f3 c1) {
+	float* f = reinterpret_cast<float*>(dst);
+	if (j == 0) {
+		*reinterpret_cast<float4*>(f) = make_float4(c0.x, c0.y, c0.z, c1.x);
+		*reinterpret_cast<float2*>(f + 4) = make_float2(c1.y, c1.z);
+	} else {
+		*reinterpret_cast<float2*>(f + 6) = make_float2(c0.x, c0.y);
+		*reinterpret_cast<float4*>(f + 8) = make_float4(c0.z, c1.x, c1.y, c1.z);
+	}
+}
+
 // evaluate_polygonal_light_shading_peters for SAMPLE_COUNT == 1 up to the
-// visibility test.  Returns the two techniques' modes; fills c and ray.  l
-// is the light whose device record is `record`.
+// visibility test.  Writes both techniques' contributions into *dst (zero
+// where a technique has none) and each traced technique's shadow ray into
+// staged[j] as soon as they are known, and returns the techniques' modes.
+// l is the light whose device record is `record`.
 template <class P>
 RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l,
-                             const float4* record, uint32_t& seed, f3 (&c)[2][2], ShadowRay (&ray)[2]) {
+                             const float4* record, uint32_t& seed, SampleRecord* dst, ShadowRay* staged) {
 	const bool fa = pr.fast_atan != 0;
 	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
 	side_flip(ltc, sd, l);
@@ -73,7 +88,11 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 		                                                  : mul(ltc.shading_to_cosine, ltc.world_to_shading),
 		                                           record, poly, fa);
 		psa[j] = vc == 0 ? 0.0f : poly.psa;
-		if (j == 0 && (vc == 0 || psa[0] == 0.0f)) return 0;
+		if (j == 0 && (vc == 0 || psa[0] == 0.0f)) {
+			store_contributions(dst, 0, splat(0.0f), splat(0.0f));
+			store_contributions(dst, 1, splat(0.0f), splat(0.0f));
+			return 0;
+		}
 		if (j == 1 && !(psa[1] > 0.0f)) break;
 		const f3 dir = sample_psa<P>(poly, get_noise_2(seed), fa, biased);
 		if (j == 0) {
@@ -96,9 +115,12 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 	const bool shadows = pr.shadows && pr.scene.triangle_count != 0;
 	uint32_t modes = 0;
 #pragma unroll 1
-	for (int j = 0; j != technique_count; ++j) {
+	for (int j = 0; j != 2; ++j) {
 		f3 dir = (j == 0) ? dir_d : dir_s;
-		if (dir.z <= 0.0f) continue;
+		if (j >= technique_count || dir.z <= 0.0f) {
+			store_contributions(dst, j, splat(0.0f), splat(0.0f));
+			continue;
+		}
 		float diffuse_density = dir.z * rcp_d;
 		float specular_density = evaluate_ltc_density<P>(ltc, dir, rcp_s);
 		f3 world_dir = transpose_mul(ltc.world_to_shading, dir);
@@ -112,6 +134,7 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 		const float other_density = j == 0 ? specular_density : diffuse_density;
 		// Outcome 0: visible iff side (unoccluded or untraced); outcome 1:
 		// occluded.
+		f3 c[2] = {splat(0.0f), splat(0.0f)};
 #pragma unroll 1
 		for (int o = 0; o != (traced ? 2 : 1); ++o) {
 			const bool visibility = (o == 0) ? side : false;
@@ -122,20 +145,16 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 			else
 				r = mis_estimate<P>(pr.mis_heuristic, integrand, own_weight, own_density, other_weight, other_density,
 				                    pr.mis_visibility_estimate);
-			if (j == 0) {
-				if (o == 0) c[0][0] = r; else c[0][1] = r;
-			} else {
-				if (o == 0) c[1][0] = r; else c[1][1] = r;
-			}
+			if (o == 0) c[0] = r; else c[1] = r;
 		}
+		store_contributions(dst, j, c[0], c[1]);
 		if (traced) {
 			// get_polygon_visibility, shading_pass.frag.glsl:112-129
 			float max_t = P::div(-plane_dot(sd.position, l.plane),
 			                     world_dir.x * l.plane[0] + world_dir.y * l.plane[1] + world_dir.z * l.plane[2]);
 			max_t -= 1e-3f;
-			const ShadowRay q{make_float4(sd.position.x, sd.position.y, sd.position.z, 0.0f),
-			                  make_float4(world_dir.x, world_dir.y, world_dir.z, max_t)};
-			if (j == 0) ray[0] = q; else ray[1] = q;
+			staged[j] = ShadowRay{make_float4(sd.position.x, sd.position.y, sd.position.z, 0.0f),
+			                      make_float4(world_dir.x, world_dir.y, world_dir.z, max_t)};
 		}
 		modes |= (traced ? kSampleTraced : kSampleFixed) << (2 * j);
 	}
@@ -185,30 +204,29 @@ template <class P> __global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOC
 		for (uint32_t f = 0; f != pr.frame_count; ++f) {
 			const size_t pf = (size_t) f * np + i;
 			uint32_t modes = 0;
-			ShadowRay ray[2];
+			int light = -1;
 			if (active) {
 				const ReservoirRecord r = pr.records[pf];
-				f3 c[2][2];
-				c[0][0] = c[0][1] = c[1][0] = c[1][1] = splat(0.0f);
-				float W = 0.0f;
-				uint32_t flags = kSampleNoLight;
+				light = r.light_index;
 				if (r.light_index >= 0) {
 					Light l;
 					load_light(pr.scene, r.light_index, l);
 					uint32_t seed = r.seed;
-					modes = psa_mis_emit<P>(sp, sd, ltc, l, light_record(pr.scene, r.light_index), seed, c, ray);
-					W = P::div(r.w_sum, (float) pr.candidate_count * r.p_hat);
+					// Contributions and staged rays go to memory inside.
+					modes = psa_mis_emit<P>(sp, sd, ltc, l, light_record(pr.scene, r.light_index), seed,
+					                        pr.samples + pf, pr.staged + 2 * pf);
+					float W = P::div(r.w_sum, (float) pr.candidate_count * r.p_hat);
 					if (r.p_hat == 0.0f) W = 0.0f;
-					flags = modes;
+					*reinterpret_cast<float2*>(reinterpret_cast<float*>(pr.samples + pf) + 12) =
+					    make_float2(W, __uint_as_float(modes));
+				} else {
+					const f3 zero[2][2] = {{splat(0.0f), splat(0.0f)}, {splat(0.0f), splat(0.0f)}};
+					store_sample(pr.samples + pf, zero, 0.0f, kSampleNoLight);
 				}
-				store_sample(pr.samples + pf, c, W, flags);
 			}
-			// Stage the rays in their pixel-frame's slots and count them for
-			// their light's bucket.
+			// Count the staged rays for their light's bucket.
 			const bool t0 = (modes & 3u) == kSampleTraced, t1 = ((modes >> 2) & 3u) == kSampleTraced;
-			if (t0) pr.staged[2 * pf] = ray[0];
-			if (t1) pr.staged[2 * pf + 1] = ray[1];
-			if (t0 || t1) atomicAdd(pr.light_rays + pr.records[pf].light_index, (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
+			if (t0 || t1) atomicAdd(pr.light_rays + light, (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
 		}
 	}
 }
