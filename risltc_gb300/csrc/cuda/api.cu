@@ -628,7 +628,8 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 	m->steps += 1;
 	const double b1 = 0.9, b2 = 0.999;
 	risltc::mlp_adam_kernel<<<64, 256, 0, stream>>>(m->d_params, m->d_grad, m->d_adam_m, m->d_adam_v, m->d_weights,
-	                                               m->parameter_count, m->learning_rate, (float) b1, (float) b2, 1e-8f,
+	                                               m->parameter_count, m->cluster_count, m->learning_rate, (float) b1,
+	                                               (float) b2, 1e-8f,
 	                                               (float) (1.0 - std::pow(b1, (double) m->steps)),
 	                                               (float) (1.0 - std::pow(b2, (double) m->steps)));
 	return cudaGetLastError();
@@ -1226,7 +1227,8 @@ static int model_upload(risltc_model_t* m, const float* host) {
 	cudaSetDevice(m->ctx->device);
 	cudaError_t e = cudaMemcpy(m->d_params, host, sizeof(float) * m->parameter_count, cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) return cuda_status(e);
-	risltc::mlp_convert_kernel<<<64, 256, 0, m->ctx->stream>>>(m->d_params, m->d_weights, m->parameter_count);
+	risltc::mlp_convert_kernel<<<64, 256, 0, m->ctx->stream>>>(m->d_params, m->d_weights, m->parameter_count,
+	                                                           m->cluster_count);
 	e = cudaGetLastError();
 	if (e == cudaSuccess) e = cudaStreamSynchronize(m->ctx->stream);
 	return cuda_status(e);
@@ -1244,7 +1246,10 @@ EXTERN_C int risltc_model_create(risltc_ctx_t* ctx, uint32_t cluster_count, uint
 	m->inv_half_extent = 1.0f;
 	cudaSetDevice(ctx->device);
 	cudaError_t e = cudaMalloc(&m->d_params, sizeof(float) * m->parameter_count);
-	if (e == cudaSuccess) e = cudaMalloc(&m->d_weights, sizeof(__nv_bfloat16) * m->parameter_count);
+	// The operand-layout weights; W3's padding rows stay zero.
+	const size_t weight_bytes = sizeof(__nv_bfloat16) * (size_t) risltc::mlp_weight_elements((int) cluster_count);
+	if (e == cudaSuccess) e = cudaMalloc(&m->d_weights, weight_bytes);
+	if (e == cudaSuccess) e = cudaMemset(m->d_weights, 0, weight_bytes);
 	for (float** buf : {&m->d_grad, &m->d_adam_m, &m->d_adam_v}) {
 		if (e == cudaSuccess) e = cudaMalloc(buf, sizeof(float) * m->parameter_count);
 		if (e == cudaSuccess) e = cudaMemset(*buf, 0, sizeof(float) * m->parameter_count);

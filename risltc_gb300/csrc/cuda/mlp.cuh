@@ -39,11 +39,34 @@ inline __host__ __device__ MlpLayout mlp_layout(int k_count) {
 	return l;
 }
 
+// The BF16 weights in the tensor cores' operand layout: W1 (64 x 144), W2
+// (64 x 64) and W3 (k_count rows, zero rows up to a multiple of 16, x 64),
+// each K-major in 8x8 core matrices (element (row, col) of a matrix with k
+// columns at byte ((row / 8) * (k / 8) + col / 8) * 128 + (row % 8) * 16 +
+// (col % 8) * 2), one after another, so that a kernel stages all three with
+// one bulk copy.
+__host__ __device__ constexpr uint32_t tc_offset(int row, int col, int k) {
+	return (uint32_t) (((row >> 3) * (k >> 3) + (col >> 3)) * 128 + (row & 7) * 16 + (col & 7) * 2);
+}
+__host__ __device__ inline int mlp_padded_clusters(int k_count) { return (k_count + 15) / 16 * 16; }
+__host__ __device__ inline int mlp_weight_elements(int k_count) {
+	return kMlpHidden * kMlpFeatures + kMlpHidden * kMlpHidden + mlp_padded_clusters(k_count) * kMlpHidden;
+}
+// Element of the operand-layout weights holding parameter j, or -1 for a bias.
+__host__ __device__ inline int mlp_weight_slot(int j, int k_count) {
+	const MlpLayout l = mlp_layout(k_count);
+	if (j >= l.w1 && j < l.b1) return (int) tc_offset((j - l.w1) / kMlpFeatures, (j - l.w1) % kMlpFeatures, kMlpFeatures) / 2;
+	const int w2_base = kMlpHidden * kMlpFeatures, w3_base = w2_base + kMlpHidden * kMlpHidden;
+	if (j >= l.w2 && j < l.b2) return w2_base + (int) tc_offset((j - l.w2) / kMlpHidden, (j - l.w2) % kMlpHidden, kMlpHidden) / 2;
+	if (j >= l.w3 && j < l.b3) return w3_base + (int) tc_offset((j - l.w3) / kMlpHidden, (j - l.w3) % kMlpHidden, kMlpHidden) / 2;
+	return -1;
+}
+
 struct MlpParams {
 	const float* gbuffer;
 	const uint32_t* primitive;
 	uint32_t width, height;
-	const __nv_bfloat16* weights;  // BF16 copy of the parameter vector (biases unused)
+	const __nv_bfloat16* weights;  // BF16 weights in the operand layout (mlp_weight_slot)
 	const float* params;           // FP32 parameter vector (biases read from here)
 	int k_count;                   // clusters, a multiple of 8
 	float center[3], inv_half_extent;
@@ -84,10 +107,13 @@ RL_DEV uint32_t pack_bf16x2(float lo, float hi) {
 	return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// FP32 parameters to their BF16 copy.
-static __global__ void mlp_convert_kernel(const float* params, __nv_bfloat16* weights, int count) {
-	for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
-		weights[j] = __float2bfloat16_rn(params[j]);
+// FP32 parameters to the BF16 operand-layout weights (zero padding rows are
+// left as the allocation's zeros).
+static __global__ void mlp_convert_kernel(const float* params, __nv_bfloat16* weights, int count, int k_count) {
+	for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+		const int slot = mlp_weight_slot(j, k_count);
+		if (slot >= 0) weights[slot] = __float2bfloat16_rn(params[j]);
+	}
 }
 
 // BF16 logits to FP32 (for inspection).
@@ -293,8 +319,8 @@ static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrai
 // Adam (Kingma & Ba 2015) on the FP32 parameters; clears the gradient and
 // refreshes the BF16 copy.  The padding features' weights stay zero.
 static __global__ void mlp_adam_kernel(float* params, float* grad, float* m, float* v, __nv_bfloat16* weights, int count,
-                                       float learning_rate, float beta1, float beta2, float epsilon, float correction1,
-                                       float correction2) {
+                                       int k_count, float learning_rate, float beta1, float beta2, float epsilon,
+                                       float correction1, float correction2) {
 	for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
 		const float g = grad[j];
 		const float mj = beta1 * m[j] + (1.0f - beta1) * g;
@@ -305,7 +331,8 @@ static __global__ void mlp_adam_kernel(float* params, float* grad, float* m, flo
 		float p = params[j];
 		if (!padding) p -= learning_rate * (mj / correction1) / (sqrtf(vj / correction2) + epsilon);
 		params[j] = p;
-		weights[j] = __float2bfloat16_rn(p);
+		const int slot = mlp_weight_slot(j, k_count);
+		if (slot >= 0) weights[slot] = __float2bfloat16_rn(p);
 		grad[j] = 0.0f;
 	}
 }

@@ -29,13 +29,6 @@ constexpr uint32_t kErrorTensorWait = 1u << 2;  // error-word bit: a tensor-core
 
 RL_DEV uint32_t smem_address(const void* p) { return (uint32_t) __cvta_generic_to_shared(p); }
 
-// Byte offset of element (row, col) of a K-major BF16 operand with k columns
-// (a multiple of 8): core matrix (row / 8, col / 8) at
-// ((row / 8) * (k / 8) + col / 8) * 128 bytes, its rows 16 bytes apart.
-__host__ __device__ constexpr uint32_t tc_offset(int row, int col, int k) {
-	return (uint32_t) (((row >> 3) * (k >> 3) + (col >> 3)) * 128 + (row & 7) * 16 + (col & 7) * 2);
-}
-
 // Shared-memory matrix descriptor of a K-major operand with k columns whose
 // first core matrix is at shared address addr (no swizzle): core matrices
 // 128 bytes apart along K (leading byte offset), 8-row groups (k / 8) * 128
@@ -95,6 +88,21 @@ RL_DEV bool tc_wait(uint32_t bar, uint32_t parity) {
 	return false;
 }
 
+// The mbarrier's phase also waits for `bytes` of asynchronous copies (one
+// arrival by this thread).
+RL_DEV void mbarrier_expect_bytes(uint32_t bar, uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bulk copy (TMA, no tensor map) of `bytes` (a multiple of 16; both
+// addresses 16-byte aligned) from global memory into this CTA's shared
+// memory, counted on the mbarrier.
+RL_DEV void bulk_copy_to_shared(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+	             "l"(src), "r"(bytes), "r"(bar)
+	             : "memory");
+}
+
 RL_DEV void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 RL_DEV void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 RL_DEV void tc_wait_load() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
@@ -110,15 +118,19 @@ RL_DEV void tc_load32(uint32_t taddr, uint32_t (&v)[32]) {
 }
 
 // Shared memory of the kernel for k_count clusters: W1, W2, W3 (rows padded
-// to a multiple of 16), A1, A2, the biases, the mbarrier and the tensor
-// memory address.
+// to a multiple of 16; together the operand-layout weights of one bulk copy),
+// A1, A2, the biases, three mbarriers (products, weights, inputs) and the
+// tensor memory address.  A tile's 10 input rows (128 floats each) are
+// staged in the first 5 KB of A2, which is free from a tile's last layer-3
+// product until the next tile's first epilogue.
 struct TcLayout {
-	uint32_t w1, w2, w3, a1, a2, b1, b2, b3, bar, slot, total;
+	uint32_t w1, w2, w3, a1, a2, b1, b2, b3, bar, slot, total, weight_bytes;
 	int k_pad;
 };
 __host__ __device__ inline TcLayout tc_layout(int k_count) {
 	TcLayout l;
-	l.k_pad = (k_count + 15) / 16 * 16;
+	l.k_pad = mlp_padded_clusters(k_count);
+	l.weight_bytes = (uint32_t) mlp_weight_elements(k_count) * 2;
 	l.w1 = 0;
 	l.w2 = l.w1 + kMlpHidden * kMlpFeatures * 2;
 	l.w3 = l.w2 + kMlpHidden * kMlpHidden * 2;
@@ -128,10 +140,14 @@ __host__ __device__ inline TcLayout tc_layout(int k_count) {
 	l.b2 = l.b1 + kMlpHidden * 4;
 	l.b3 = l.b2 + kMlpHidden * 4;
 	l.bar = (l.b3 + (uint32_t) l.k_pad * 4 + 7) / 8 * 8;
-	l.slot = l.bar + 8;
+	l.slot = l.bar + 3 * 8;
 	l.total = l.slot + 8;
 	return l;
 }
+static_assert(kMlpInputs * kTcRows * 4 <= kTcRows * kMlpHidden * 2, "inputs fit in A2");
+
+// G-buffer plane of MLP input k (position, normal, outgoing, roughness).
+RL_DEV int mlp_input_plane(int k) { return k < 9 ? k : 16; }
 
 static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(MlpParams pr) {
 	extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -143,28 +159,39 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 	float* b1 = reinterpret_cast<float*>(tc_smem + tl.b1);
 	float* b2 = reinterpret_cast<float*>(tc_smem + tl.b2);
 	float* b3 = reinterpret_cast<float*>(tc_smem + tl.b3);
-	// Weights into their operand layouts (W3 rows past k_count are zero).
-	for (int j = tid; j < kMlpHidden * kMlpFeatures; j += kTcThreads)
-		*reinterpret_cast<__nv_bfloat16*>(tc_smem + tl.w1 + tc_offset(j / kMlpFeatures, j % kMlpFeatures, kMlpFeatures)) =
-		    pr.weights[lay.w1 + j];
-	for (int j = tid; j < kMlpHidden * kMlpHidden; j += kTcThreads)
-		*reinterpret_cast<__nv_bfloat16*>(tc_smem + tl.w2 + tc_offset(j / kMlpHidden, j % kMlpHidden, kMlpHidden)) =
-		    pr.weights[lay.w2 + j];
-	for (int j = tid; j < tl.k_pad * kMlpHidden; j += kTcThreads) {
-		const int o = j / kMlpHidden, f = j % kMlpHidden;
-		*reinterpret_cast<__nv_bfloat16*>(tc_smem + tl.w3 + tc_offset(o, f, kMlpHidden)) =
-		    o < k_count ? pr.weights[lay.w3 + j] : __float2bfloat16_rn(0.0f);
-	}
+	const float* inputs = reinterpret_cast<const float*>(tc_smem + tl.a2);  // [10][128] while staged
 	for (int j = tid; j < kMlpHidden; j += kTcThreads) {
 		b1[j] = pr.params[lay.b1 + j];
 		b2[j] = pr.params[lay.b2 + j];
 	}
 	for (int j = tid; j < tl.k_pad; j += kTcThreads) b3[j] = j < k_count ? pr.params[lay.b3 + j] : 0.0f;
-	const uint32_t bar = base + tl.bar;
+	const uint32_t bar = base + tl.bar, bar_weights = bar + 8, bar_inputs = bar + 16;
+	const uint32_t np = pr.width * pr.height;
+	const uint32_t tiles = (np + kTcRows - 1) / kTcRows;
+	// A tile's input rows come by bulk copy when every row is 16-byte aligned
+	// and a multiple of 16 bytes long, else by plain loads.
+	const bool bulk_inputs = np % 4 == 0 && (reinterpret_cast<uintptr_t>(pr.gbuffer) & 15) == 0;
+	// Bulk copies issued and waited for on the inputs' mbarrier (the same on
+	// every thread: the issue decisions are uniform).
+	uint32_t inputs_issued = 0, inputs_waited = 0;
+	auto fetch_inputs = [&](uint32_t tile) {
+		if (tid == 0) {
+			const uint32_t p0 = tile * kTcRows, rows = min((uint32_t) kTcRows, np - p0);
+			mbarrier_expect_bytes(bar_inputs, kMlpInputs * rows * 4);
+			for (int k = 0; k != kMlpInputs; ++k)
+				bulk_copy_to_shared(base + tl.a2 + k * kTcRows * 4, pr.gbuffer + (size_t) mlp_input_plane(k) * np + p0,
+				                    rows * 4, bar_inputs);
+		}
+		++inputs_issued;
+	};
 	if (tid == 0) {
-		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+		for (int k = 0; k != 3; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar + 8 * k) : "memory");
 		asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+		// The weights in one bulk copy.
+		mbarrier_expect_bytes(bar_weights, tl.weight_bytes);
+		bulk_copy_to_shared(base + tl.w1, pr.weights, tl.weight_bytes, bar_weights);
 	}
+	if (bulk_inputs && blockIdx.x < tiles) fetch_inputs(blockIdx.x);  // the first tile's inputs
 	if (warp == 0) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(base + tl.slot),
 		             "r"(kTcColumns)
@@ -178,10 +205,10 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 	const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tc_smem + tl.slot);
 	const uint32_t d12 = tmem, d3 = tmem + 64;
 	const uint32_t lane_base = (warp * 32) << 16;  // this warp's tensor-memory lanes
-	const uint32_t np = pr.width * pr.height;
-	const uint32_t tiles = (np + kTcRows - 1) / kTcRows;
 	uint32_t parity = 0;
-	bool failed = false;
+	bool product_pending = false;
+	const bool weights_ok = __syncthreads_or(!tc_wait(bar_weights, 0)) == 0;
+	bool failed = !weights_ok;
 	// One product group: issued by thread 0, then every thread waits for it.
 	// With pr.skip_issue (fault injection) nothing is issued or committed, so
 	// the wait runs out.
@@ -193,6 +220,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 		const bool ok = tc_wait(bar, parity);
 		parity ^= 1u;
 		failed = __syncthreads_or(!ok) != 0;
+		product_pending = failed && !pr.skip_issue;
 		tc_fence_after();
 	};
 	// Epilogue of a hidden layer: row tid of D (64 columns) + bias, ReLU,
@@ -222,12 +250,27 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 	};
 	for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
 		const uint32_t p0 = tile * kTcRows;
+		if (bulk_inputs) {
+			// This tile's input rows (issued during the previous tile).
+			failed = __syncthreads_or(!tc_wait(bar_inputs, inputs_waited & 1u)) != 0;
+			if (failed) break;
+			++inputs_waited;
+		}
 		// Encode the tile's pixels into A1.
 		for (int idx = tid; idx < kTcRows * kMlpInputs; idx += kTcThreads) {
 			const int r = idx / kMlpInputs, input = idx % kMlpInputs;
 			const uint32_t i = p0 + (uint32_t) r;
+			float x = 0.0f;
+			if (i < np) {
+				if (bulk_inputs) {
+					x = inputs[input * kTcRows + r];
+					if (input < 3) x = (x - pr.center[input]) * pr.inv_half_extent;
+				} else {
+					x = mlp_input(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, input);
+				}
+			}
 			float e[13];
-			mlp_encode(i < np ? mlp_input(pr.gbuffer, np, i, pr.center, pr.inv_half_extent, input) : 0.0f, e);
+			mlp_encode(x, e);
 #pragma unroll
 			for (int kind = 0; kind != 13; ++kind)
 				*reinterpret_cast<__nv_bfloat16*>(tc_smem + tl.a1 + tc_offset(r, input * 13 + kind, kMlpFeatures)) =
@@ -265,6 +308,9 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 					       tc_instruction(kTcRows, n), k > 0);
 			});
 			if (failed) break;
+			// After the tile's last product A2 is free: the next tile's inputs
+			// arrive there while this tile's logits are written.
+			if (c0 + kTcChunk >= tl.k_pad && bulk_inputs && tile + gridDim.x < tiles) fetch_inputs(tile + gridDim.x);
 			for (int c = 0; c < n; c += 32) {
 				uint32_t v[32];
 				tc_load32(d3 + lane_base + (uint32_t) c, v);
@@ -293,8 +339,12 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_logits_tc_kernel(Mlp
 		}
 	}
 	if (failed) {
+		// Record the timeout, then wait (bounded) for whatever is still in
+		// flight: a product, the weights' copy, input copies.
 		if (tid == 0) atomicOr(pr.error, kErrorTensorWait);
-		if (!pr.skip_issue) tc_wait(bar, parity ^ 1u);  // the product still in flight (its phase), bounded
+		if (product_pending) tc_wait(bar, parity ^ 1u);
+		if (!weights_ok) tc_wait(bar_weights, 0);
+		while (inputs_waited < inputs_issued) tc_wait(bar_inputs, inputs_waited++ & 1u);
 	}
 	tc_fence_before();
 	__syncthreads();

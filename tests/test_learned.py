@@ -170,6 +170,30 @@ def mean_kl(targets, logits):
 
 
 @pytest.mark.gpu
+def test_model_logits_unaligned_frame(gpu):
+    """A frame whose pixel count is not a multiple of 4: the inputs come by
+    plain loads instead of bulk copies."""
+    import torch
+    import risltc_gb300 as rl
+    sc = gd.scene("hf")
+    n = sc["width"] * sc["height"] - 1
+    assert n % 4 != 0
+    g_host = np.ascontiguousarray(sc["gbuffer"][:, :n])
+    ctx = rl.Context(0)
+    model = rl.Model(ctx, 64, seed=9)
+    params = model.get_params()
+    center, half = (0.0, 0.0, 1.0), 6.0
+    model.set_input_transform(center, half)
+    got = model.logits(torch.from_numpy(g_host).cuda(), n, 1).cpu().numpy()
+    ctx.check()
+    model.close()
+    ctx.close()
+    want = reference_logits(params, 64, encode(g_host, center, half))
+    err = np.abs(got - want)
+    assert err.max() <= 0.08 * np.abs(want).max()
+
+
+@pytest.mark.gpu
 def test_online_training_moves_the_proposal_towards_the_targets(gpu):
     import torch
     import risltc_gb300 as rl
