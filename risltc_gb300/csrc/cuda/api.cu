@@ -225,7 +225,9 @@ int reserve_wavefront(risltc_ctx_t* ctx, size_t pixel_frames, size_t light_count
 		cudaFree(ctx->d_light_rays);
 		ctx->d_light_rays = nullptr;
 		ctx->light_capacity = 0;
-		if ((e = cudaMalloc(&ctx->d_light_rays, light_count * sizeof(uint32_t))) != cudaSuccess) return cuda_status(e);
+		if ((e = cudaMalloc(&ctx->d_light_rays, light_count * risltc::kLightCounterStride * sizeof(uint32_t))) !=
+		    cudaSuccess)
+			return cuda_status(e);
 		ctx->light_capacity = light_count;
 	}
 	if (pixel_frames <= ctx->wavefront_capacity) return RISLTC_OK;
@@ -1079,7 +1081,7 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 			sc.rays = ctx->d_rays + 2 * w_off;
 			sc.hits = ctx->d_hits + 2 * w_off;
 			sc.ray_count = ctx->d_ray_count + 2 * q_off;
-			sc.light_rays = ctx->d_light_rays + l_off;
+			sc.light_rays = ctx->d_light_rays + l_off * risltc::kLightCounterStride;
 			w_off += pf;
 			l_off += (size_t) it.scene->view.light_count;
 			++q_off;

@@ -226,7 +226,7 @@ template <class P> __global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOC
 			}
 			// Count the staged rays for their light's bucket.
 			const bool t0 = (modes & 3u) == kSampleTraced, t1 = ((modes >> 2) & 3u) == kSampleTraced;
-			if (t0 || t1) atomicAdd(pr.light_rays + light, (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
+			if (t0 || t1) atomicAdd(pr.light_rays + (size_t) light * kLightCounterStride, (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
 		}
 	}
 }
@@ -243,7 +243,7 @@ static __global__ void __launch_bounds__(1024) light_bucket_scan_kernel(uint32_t
 	uint32_t carry = 0;
 	for (uint32_t base = 0; base < light_count; base += 1024) {
 		const uint32_t i = base + threadIdx.x;
-		const uint32_t v = i < light_count ? light_rays[i] : 0u;
+		const uint32_t v = i < light_count ? light_rays[(size_t) i * kLightCounterStride] : 0u;
 		uint32_t incl = v;
 #pragma unroll
 		for (int d = 1; d < 32; d <<= 1) {
@@ -264,7 +264,7 @@ static __global__ void __launch_bounds__(1024) light_bucket_scan_kernel(uint32_t
 			if (lane == 31) chunk_total = wi;
 		}
 		__syncthreads();
-		if (i < light_count) light_rays[i] = carry + warp_offset[warp] + incl - v;
+		if (i < light_count) light_rays[(size_t) i * kLightCounterStride] = carry + warp_offset[warp] + incl - v;
 		carry += chunk_total;
 		__syncthreads();
 	}
@@ -286,7 +286,8 @@ static __global__ void __launch_bounds__(128) shadow_scatter_kernel(RisParams pr
 		if (flags & kSampleNoLight) continue;
 		const bool t0 = (flags & 3u) == kSampleTraced, t1 = ((flags >> 2) & 3u) == kSampleTraced;
 		if (!t0 && !t1) continue;
-		uint32_t at = atomicAdd(pr.light_rays + pr.records[pf].light_index, (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
+		uint32_t at = atomicAdd(pr.light_rays + (size_t) pr.records[pf].light_index * kLightCounterStride,
+		                        (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
 		const uint32_t slot = 2u * (uint32_t) pf;
 		if (t0) {
 			ShadowRay q = pr.staged[2 * pf];
