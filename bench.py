@@ -70,6 +70,9 @@ def parse():
     p.add_argument("--reference-spp", type=int, default=4096)
     p.add_argument("--shadowed-target", type=float, default=0.5,
                    help="weight of the shadowed (visibility) part of the learned proposal's training target")
+    p.add_argument("--learning-rate", type=float, default=5e-3,
+                   help="equal-mse: the learned proposal's Adam step (measured: 1e-3 trains too slowly in 64 frames, "
+                        "5e-3 and 1e-2 equally well)")
     p.add_argument("--sweep-candidates", default="",
                    help="equal-mse: also measure every method at these candidate counts (comma-separated); plain "
                         "RIS at --candidates stays the MSE level to reach")
@@ -475,7 +478,7 @@ def run_equal_mse(a):
     reference = acc / (16 * (a.reference_spp // 16))
     ctx.check()
     # Online training of the model (1 spp per call, its own candidates).
-    model.set_training(True, learning_rate=2e-3, pixel_stride=16)
+    model.set_training(True, learning_rate=a.learning_rate, pixel_stride=16)
     model.set_target_mix(a.shadowed_target)
     out = torch.empty((P, 3), dtype=torch.float32, device="cuda")
     seed = 20_000_000
@@ -540,7 +543,7 @@ def run_equal_mse(a):
                                "clusters, %dk occluder triangles, M=%d, MSE at %d spp against a %d-spp FP64 plain-RIS "
                                "reference" % (hs.width, hs.height, hs.light_count, a.clusters, a.triangles // 1000,
                                               a.candidates, a.spp, a.reference_spp),
-                   "train_frames": a.train_frames, "train_ms_per_frame": train_ms,
+                   "train_frames": a.train_frames, "train_ms_per_frame": train_ms, "learning_rate": a.learning_rate,
                    "shadowed_target": a.shadowed_target},
         "plain_ms_to_equal_mse": base["ms_to_plain_mse"],
         "speedup_vs_plain": base["ms_to_plain_mse"] / results["learned"]["ms_to_plain_mse"],
