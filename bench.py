@@ -73,6 +73,10 @@ def parse():
     p.add_argument("--learning-rate", type=float, default=5e-3,
                    help="equal-mse: the learned proposal's Adam step (measured: 1e-3 trains too slowly in 64 frames, "
                         "5e-3 and 1e-2 equally well)")
+    p.add_argument("--train-stride", type=int, default=16, help="equal-mse: every n-th pixel trains the model")
+    p.add_argument("--uniform-fraction", type=float, default=0.05,
+                   help="equal-mse: weight of uniform light choice in the proposals' defensive mixture (measured on "
+                        "960x540: 0.05 gives a lower MSE than 0.1 for both proposals)")
     p.add_argument("--sweep-candidates", default="",
                    help="equal-mse: also measure every method at these candidate counts (comma-separated); plain "
                         "RIS at --candidates stays the MSE level to reach")
@@ -467,8 +471,8 @@ def run_equal_mse(a):
     g = torch.from_numpy(hs.gbuffer).cuda()
     prim = torch.from_numpy(hs.primitive.view(np.int32)).cuda()
     plain = rl.settings(candidates=a.candidates)
-    clusters = rl.settings(candidates=a.candidates, proposal="clusters", proposal_uniform_fraction=0.1)
-    learned = rl.settings(candidates=a.candidates, proposal="learned", proposal_uniform_fraction=0.1)
+    clusters = rl.settings(candidates=a.candidates, proposal="clusters", proposal_uniform_fraction=a.uniform_fraction)
+    learned = rl.settings(candidates=a.candidates, proposal="learned", proposal_uniform_fraction=a.uniform_fraction)
     # Reference: FP64 running sums of plain RIS.
     acc = torch.zeros((P, 3), dtype=torch.float64, device="cuda")
     seed = 10_000_000
@@ -478,7 +482,7 @@ def run_equal_mse(a):
     reference = acc / (16 * (a.reference_spp // 16))
     ctx.check()
     # Online training of the model (1 spp per call, its own candidates).
-    model.set_training(True, learning_rate=a.learning_rate, pixel_stride=16)
+    model.set_training(True, learning_rate=a.learning_rate, pixel_stride=a.train_stride)
     model.set_target_mix(a.shadowed_target)
     out = torch.empty((P, 3), dtype=torch.float32, device="cuda")
     seed = 20_000_000
@@ -544,6 +548,7 @@ def run_equal_mse(a):
                                "reference" % (hs.width, hs.height, hs.light_count, a.clusters, a.triangles // 1000,
                                               a.candidates, a.spp, a.reference_spp),
                    "train_frames": a.train_frames, "train_ms_per_frame": train_ms, "learning_rate": a.learning_rate,
+                   "train_stride": a.train_stride, "uniform_fraction": a.uniform_fraction,
                    "shadowed_target": a.shadowed_target},
         "plain_ms_to_equal_mse": base["ms_to_plain_mse"],
         "speedup_vs_plain": base["ms_to_plain_mse"] / results["learned"]["ms_to_plain_mse"],
