@@ -381,6 +381,21 @@ EXTERN_C int risltc_model_set_training(risltc_model_t* model, int enable, float 
    light's cluster, which makes the proposal learn visibility.  The shadowed
    part needs shadows on and one sample per technique. */
 EXTERN_C int risltc_model_set_target_mix(risltc_model_t* model, float shadowed_weight);
+/* How training steps run (flags, default 0): on the tensor cores (tcgen05,
+   BF16 operands, FP32 accumulation) for models of up to 256 clusters, in
+   FP32 on the CUDA cores beyond that.  RISLTC_TRAIN_CUDA_CORES: the FP32
+   CUDA-core kernel for every model.  RISLTC_TRAIN_ACCUMULATE_ONLY: each
+   training call adds its gradient to the model's gradient vector and takes
+   no Adam step (risltc_model_apply_update takes it). */
+#define RISLTC_TRAIN_CUDA_CORES 1u
+#define RISLTC_TRAIN_ACCUMULATE_ONLY 2u
+EXTERN_C int risltc_model_set_training_flags(risltc_model_t* model, uint32_t flags);
+/* The accumulated gradient (risltc_model_parameter_count floats, host
+   memory; synchronises the context's stream), reset to zero if clear. */
+EXTERN_C int risltc_model_get_gradient(risltc_model_t* model, float* gradient, int clear);
+/* One Adam step on the accumulated gradient, which it resets
+   (stream-ordered on the context's stream). */
+EXTERN_C int risltc_model_apply_update(risltc_model_t* model);
 /* Inputs: position (p - center) / half_extent. */
 EXTERN_C int risltc_model_set_input_transform(risltc_model_t* model, const float center[3], float half_extent);
 /* The model the scene's learned proposal uses (its cluster count must match
@@ -560,6 +575,8 @@ EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx);
    next risltc_ctx_check reports RISLTC_ERROR_DEVICE_TIMEOUT; the context stays
    usable.  Nothing faults, traps or hangs. */
 #define RISLTC_FAULT_TENSOR_WAIT 1u
+/* The same for the next tensor-core training launch. */
+#define RISLTC_FAULT_TRAIN_TENSOR_WAIT 2u
 EXTERN_C int risltc_ctx_inject_fault(risltc_ctx_t* ctx, uint32_t faults);
 EXTERN_C const char* risltc_status_string(int status);
 

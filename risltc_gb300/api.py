@@ -81,6 +81,14 @@ class Context:
         self._h = ctypes.c_void_p()
         check(self._lib.risltc_ctx_create(ctypes.byref(self._h), device, ctypes.c_void_p(stream)), "risltc_ctx_create")
         self.device = device
+        # (destroy function, handle) of the scenes and models made on this
+        # context: closing it destroys them first, whatever order the
+        # interpreter runs finalizers in at exit (a finalizer of a garbage
+        # cycle may run before those of the objects that refer to it).
+        self._owned = []
+
+    def _adopt(self, destroy, handle):
+        self._owned.append((destroy, handle))
 
     @property
     def handle(self):
@@ -89,10 +97,12 @@ class Context:
     def check(self):
         check(self._lib.risltc_ctx_check(self._h), "risltc_ctx_check")
 
-    def inject_fault(self, tensor_wait=False):
+    def inject_fault(self, tensor_wait=False, train_tensor_wait=False):
         """risltc_ctx_inject_fault: host-made faults for tests of the failure
-        paths (see include/risltc.h)."""
-        check(self._lib.risltc_ctx_inject_fault(self._h, 1 if tensor_wait else 0), "risltc_ctx_inject_fault")
+        paths (see include/risltc.h): the next logits launch (tensor_wait) or
+        tensor-core training launch (train_tensor_wait) issues no products."""
+        faults = (1 if tensor_wait else 0) | (2 if train_tensor_wait else 0)
+        check(self._lib.risltc_ctx_inject_fault(self._h, faults), "risltc_ctx_inject_fault")
 
     def profile(self, enable=True):
         """Per-kernel CUDA-event times (ms) of the shading calls since the last
@@ -107,6 +117,11 @@ class Context:
 
     def close(self):
         if self._h:
+            for destroy, handle in reversed(self._owned):
+                if handle:
+                    destroy(handle)
+                    handle.value = None
+            self._owned.clear()
             self._lib.risltc_ctx_destroy(self._h)
             self._h = ctypes.c_void_p()
 
@@ -139,6 +154,7 @@ class Scene:
             ctx.handle, lights.ctypes.data_as(_native.c_float_p), lights.shape[0], max_vertex_count,
             ctypes.byref(table), None if tris is None else tris.ctypes.data_as(_native.c_float_p),
             0 if tris is None else tris.shape[0], ctypes.byref(self._h)), "risltc_scene_create")
+        ctx._adopt(self._lib.risltc_scene_destroy, self._h)
         self.light_count = lights.shape[0]
 
     @classmethod
@@ -165,7 +181,7 @@ class Scene:
     def close(self):
         if self._h:
             self._lib.risltc_scene_destroy(self._h)
-            self._h = ctypes.c_void_p()
+            self._h.value = None  # also in the context's list
 
     def __del__(self):
         try:
@@ -184,6 +200,7 @@ class Model:
         self._h = ctypes.c_void_p()
         check(self._lib.risltc_model_create(ctx.handle, cluster_count, seed, ctypes.byref(self._h)),
               "risltc_model_create")
+        ctx._adopt(self._lib.risltc_model_destroy, self._h)
 
     @property
     def handle(self):
@@ -212,6 +229,25 @@ class Model:
     def set_target_mix(self, shadowed_weight):
         check(self._lib.risltc_model_set_target_mix(self._h, float(shadowed_weight)), "risltc_model_set_target_mix")
 
+    TRAIN_CUDA_CORES = 1
+    TRAIN_ACCUMULATE_ONLY = 2
+
+    def set_training_flags(self, cuda_cores=False, accumulate_only=False):
+        """risltc_model_set_training_flags: cuda_cores trains with the FP32
+        CUDA-core kernel instead of the tensor cores; accumulate_only adds each
+        step's gradient without an Adam step (apply_update takes it)."""
+        flags = (self.TRAIN_CUDA_CORES if cuda_cores else 0) | (self.TRAIN_ACCUMULATE_ONLY if accumulate_only else 0)
+        check(self._lib.risltc_model_set_training_flags(self._h, flags), "risltc_model_set_training_flags")
+
+    def get_gradient(self, clear=False):
+        out = np.zeros(self.parameter_count, np.float32)
+        check(self._lib.risltc_model_get_gradient(self._h, out.ctypes.data_as(_native.c_float_p), int(clear)),
+              "risltc_model_get_gradient")
+        return out
+
+    def apply_update(self):
+        check(self._lib.risltc_model_apply_update(self._h), "risltc_model_apply_update")
+
     def set_input_transform(self, center, half_extent):
         c = np.ascontiguousarray(center, np.float32)
         check(self._lib.risltc_model_set_input_transform(self._h, c.ctypes.data_as(_native.c_float_p),
@@ -229,7 +265,7 @@ class Model:
     def close(self):
         if self._h:
             self._lib.risltc_model_destroy(self._h)
-            self._h = ctypes.c_void_p()
+            self._h.value = None  # also in the context's list
 
     def __del__(self):
         try:

@@ -10,6 +10,7 @@
 #include "gbuffer.cuh"
 #include "mlp.cuh"
 #include "mlp_tc.cuh"
+#include "mlp_train_tc.cuh"
 #include "ris_binned.cuh"
 #include "ris_wavefront.cuh"
 
@@ -118,6 +119,7 @@ struct risltc_model_s {
 	uint32_t pixel_stride;
 	uint32_t steps;
 	float shadowed_weight;
+	uint32_t training_flags;     // RISLTC_TRAIN_*
 	float* d_shaded;             // frame 0's shaded luminance of the training pixels
 	size_t shaded_capacity;
 };
@@ -581,6 +583,19 @@ int reserve_logits(risltc_ctx_t* ctx, size_t need) {
 	return RISLTC_OK;
 }
 
+// One Adam step (Kingma & Ba 2015, beta 0.9 / 0.999) on the model's
+// accumulated gradient, which it clears (stream-ordered).
+cudaError_t launch_adam(risltc_model_t* m, cudaStream_t stream) {
+	m->steps += 1;
+	const double b1 = 0.9, b2 = 0.999;
+	risltc::mlp_adam_kernel<<<64, 256, 0, stream>>>(m->d_params, m->d_grad, m->d_adam_m, m->d_adam_v, m->d_weights,
+	                                               m->parameter_count, m->cluster_count, m->learning_rate, (float) b1,
+	                                               (float) b2, 1e-8f,
+	                                               (float) (1.0 - std::pow(b1, (double) m->steps)),
+	                                               (float) (1.0 - std::pow(b2, (double) m->steps)));
+	return cudaGetLastError();
+}
+
 // One training step of the scene's model on frame 0's candidates of the
 // training pixels, then an Adam update (stream-ordered).
 cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_scene_t* scene,
@@ -612,29 +627,37 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 	t.shaded = shaded;
 	t.records = reinterpret_cast<const int4*>(records);
 	t.shadowed_weight = m->shadowed_weight;
+	t.weights = m->d_weights;
+	t.error = ctx->d_error;
 	static std::atomic<uint64_t> configured{0};
 	const uint64_t bit = 1ull << (ctx->device & 63);
 	if (!(configured.load() & bit)) {
 		cudaError_t e = cudaFuncSetAttribute(risltc::mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                                     (int) risltc::mlp_train_smem_bytes(risltc::kMaxClusters));
+		if (e == cudaSuccess)
+			e = cudaFuncSetAttribute(risltc::mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                         (int) risltc::kTtSmemBytes);
 		if (e != cudaSuccess) return e;
 		configured.fetch_or(bit);
 	}
-	// Two blocks per SM where their shared memory fits (up to about 500
-	// clusters), one otherwise.
-	const int blocks = (int) std::min<uint32_t>((n_train + risltc::kTrainPixels - 1) / risltc::kTrainPixels,
-	                                            (uint32_t) ctx->sm_count * 2);
-	risltc::mlp_train_kernel<<<blocks, risltc::kTrainThreads, risltc::mlp_train_smem_bytes(m->cluster_count), stream>>>(t);
+	if (m->cluster_count <= risltc::kTtMaxClusters && !(m->training_flags & RISLTC_TRAIN_CUDA_CORES)) {
+		// One CTA per SM (its shared memory and all 512 tensor-memory columns).
+		t.skip_issue = (ctx->inject & RISLTC_FAULT_TRAIN_TENSOR_WAIT) ? 1u : 0u;
+		ctx->inject &= ~(uint32_t) RISLTC_FAULT_TRAIN_TENSOR_WAIT;
+		const int blocks = (int) std::min<uint32_t>((n_train + risltc::kTcRows - 1) / risltc::kTcRows,
+		                                            (uint32_t) ctx->sm_count);
+		risltc::mlp_train_tc_kernel<<<blocks, risltc::kTcThreads, risltc::kTtSmemBytes, stream>>>(t);
+	} else {
+		// Two blocks per SM where their shared memory fits (up to about 500
+		// clusters), one otherwise.
+		const int blocks = (int) std::min<uint32_t>((n_train + risltc::kTrainPixels - 1) / risltc::kTrainPixels,
+		                                            (uint32_t) ctx->sm_count * 2);
+		risltc::mlp_train_kernel<<<blocks, risltc::kTrainThreads, risltc::mlp_train_smem_bytes(m->cluster_count),
+		                           stream>>>(t);
+	}
 	cudaError_t e = cudaGetLastError();
-	if (e != cudaSuccess) return e;
-	m->steps += 1;
-	const double b1 = 0.9, b2 = 0.999;
-	risltc::mlp_adam_kernel<<<64, 256, 0, stream>>>(m->d_params, m->d_grad, m->d_adam_m, m->d_adam_v, m->d_weights,
-	                                               m->parameter_count, m->cluster_count, m->learning_rate, (float) b1,
-	                                               (float) b2, 1e-8f,
-	                                               (float) (1.0 - std::pow(b1, (double) m->steps)),
-	                                               (float) (1.0 - std::pow(b2, (double) m->steps)));
-	return cudaGetLastError();
+	if (e != cudaSuccess || (m->training_flags & RISLTC_TRAIN_ACCUMULATE_ONLY)) return e;
+	return launch_adam(m, stream);
 }
 
 // The model's logits for every pixel of the G-buffer into logits.
@@ -1179,7 +1202,8 @@ EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, 
 }
 
 EXTERN_C int risltc_ctx_inject_fault(risltc_ctx_t* ctx, uint32_t faults) {
-	if (!ctx || (faults & ~(uint32_t) RISLTC_FAULT_TENSOR_WAIT)) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (!ctx || (faults & ~(uint32_t) (RISLTC_FAULT_TENSOR_WAIT | RISLTC_FAULT_TRAIN_TENSOR_WAIT)))
+		return RISLTC_ERROR_INVALID_ARGUMENT;
 	ctx->inject |= faults;
 	return RISLTC_OK;
 }
@@ -1364,6 +1388,29 @@ EXTERN_C int risltc_model_set_target_mix(risltc_model_t* model, float shadowed_w
 	if (!model || !(shadowed_weight >= 0.0f && shadowed_weight <= 1.0f)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	model->shadowed_weight = shadowed_weight;
 	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_model_set_training_flags(risltc_model_t* model, uint32_t flags) {
+	if (!model || (flags & ~(uint32_t) (RISLTC_TRAIN_CUDA_CORES | RISLTC_TRAIN_ACCUMULATE_ONLY)))
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	model->training_flags = flags;
+	return RISLTC_OK;
+}
+
+EXTERN_C int risltc_model_get_gradient(risltc_model_t* model, float* gradient, int clear) {
+	if (!model || !gradient) return RISLTC_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(model->ctx->device);
+	cudaError_t e = cudaStreamSynchronize(model->ctx->stream);
+	if (e == cudaSuccess)
+		e = cudaMemcpy(gradient, model->d_grad, sizeof(float) * model->parameter_count, cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess && clear) e = cudaMemset(model->d_grad, 0, sizeof(float) * model->parameter_count);
+	return cuda_status(e);
+}
+
+EXTERN_C int risltc_model_apply_update(risltc_model_t* model) {
+	if (!model) return RISLTC_ERROR_INVALID_ARGUMENT;
+	cudaSetDevice(model->ctx->device);
+	return cuda_status(launch_adam(model, model->ctx->stream));
 }
 
 // ------------------------------------------------------------- G-buffers --

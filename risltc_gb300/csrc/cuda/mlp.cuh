@@ -10,7 +10,8 @@
 //
 // Weights are BF16 for inference (each layer stored [out][in]), biases FP32.
 // The forward pass runs on the tcgen05 tensor cores (mlp_tc.cuh); online
-// training (below) runs in FP32 on the CUDA cores.
+// training runs there too for up to 256 clusters (mlp_train_tc.cuh), and in
+// FP32 on the CUDA cores (below) for larger models or on request.
 #pragma once
 #include <cuda_bf16.h>
 #include "proposal.cuh"
@@ -107,12 +108,18 @@ RL_DEV uint32_t pack_bf16x2(float lo, float hi) {
 	return *reinterpret_cast<const uint32_t*>(&v);
 }
 
+// Whether parameter j is a weight of one of layer 1's padding features
+// (130..143), whose BF16 copy is always zero.
+__host__ __device__ inline bool mlp_padding_weight(int j) {
+	return j < kMlpHidden * kMlpFeatures && j % kMlpFeatures >= kMlpInputs * 13;
+}
+
 // FP32 parameters to the BF16 operand-layout weights (zero padding rows are
 // left as the allocation's zeros).
 static __global__ void mlp_convert_kernel(const float* params, __nv_bfloat16* weights, int count, int k_count) {
 	for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
 		const int slot = mlp_weight_slot(j, k_count);
-		if (slot >= 0) weights[slot] = __float2bfloat16_rn(params[j]);
+		if (slot >= 0) weights[slot] = __float2bfloat16_rn(mlp_padding_weight(j) ? 0.0f : params[j]);
 	}
 }
 
@@ -175,6 +182,10 @@ struct MlpTrainParams {
 	const float* shaded;
 	const int4* records;
 	float shadowed_weight;
+	// Read by the tensor-core kernel only.
+	const __nv_bfloat16* weights;  // BF16 weights in the operand layout
+	uint32_t* error;               // the context's error word
+	uint32_t skip_issue;           // fault injection: issue no tensor-core products
 };
 
 inline size_t mlp_train_smem_bytes(int k_count) {
@@ -327,12 +338,12 @@ static __global__ void mlp_adam_kernel(float* params, float* grad, float* m, flo
 		const float vj = beta2 * v[j] + (1.0f - beta2) * g * g;
 		m[j] = mj;
 		v[j] = vj;
-		const bool padding = j < kMlpHidden * kMlpFeatures && j % kMlpFeatures >= kMlpInputs * 13;
+		const bool padding = mlp_padding_weight(j);
 		float p = params[j];
 		if (!padding) p -= learning_rate * (mj / correction1) / (sqrtf(vj / correction2) + epsilon);
 		params[j] = p;
 		const int slot = mlp_weight_slot(j, k_count);
-		if (slot >= 0) weights[slot] = __float2bfloat16_rn(p);
+		if (slot >= 0) weights[slot] = __float2bfloat16_rn(padding ? 0.0f : p);
 		grad[j] = 0.0f;
 	}
 }

@@ -97,3 +97,20 @@ def test_arguments_past_the_limits_are_rejected(rl):
     bad[3, 4] = np.nan
     with pytest.raises(rlm.RisltcError):
         rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, bad)
+
+
+def test_closing_the_context_first_destroys_its_scenes_and_models(rl):
+    """Closing a context destroys the scenes and models made on it first, so
+    their own close (or finalizer, in any order at interpreter exit) never
+    reaches a destroyed context."""
+    rlm, _, torch = rl
+    ctx = rlm.Context(0)
+    sc = heightfield(16, 8, 16, 100, seed=9)
+    l0, l1, k = gd.ltc()
+    scene = rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    model = rlm.Model(ctx, 8, seed=1)
+    ctx.close()
+    assert not scene.handle and not model.handle
+    scene.close()
+    model.close()
+    del scene, model, ctx

@@ -249,3 +249,110 @@ def test_tensor_wait_timeout_is_reported_and_the_context_survives(gpu):
     assert np.array_equal(again, good)
     model.close()
     ctx.close()
+
+
+def gradient_blocks(k):
+    """Slices of the parameter vector: W1 (real features), b1, W2, b2, W3, b3."""
+    w1 = np.arange(64 * 144).reshape(64, 144)[:, :130].ravel()
+    o = 64 * 144
+    return [("w1", w1), ("b1", slice(o, o + 64)), ("w2", slice(o + 64, o + 64 + 4096)),
+            ("b2", slice(o + 4160, o + 4224)), ("w3", slice(o + 4224, o + 4224 + 64 * k)),
+            ("b3", slice(o + 4224 + 64 * k, o + 4224 + 65 * k))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("k", [8, 72, 256])
+def test_tensor_core_training_gradient_matches_cuda_cores(gpu, k):
+    """One training step's gradient from the tcgen05 kernel (BF16 weights,
+    activations and logit gradients, FP32 accumulation over the CTA's tiles)
+    against the FP32 CUDA-core kernel, on the same frame and candidates with
+    the shadowed target part on: each parameter block agrees within 5% of
+    its largest entry and the two vectors correlate above 0.995; with
+    accumulate_only the parameters do not move until apply_update."""
+    import torch
+    import risltc_gb300 as rl
+    hs = rl.scenes.heightfield(160, 96, light_count=2048 if k > 8 else 256, triangle_count=3000, seed=11,
+                               vertex_counts=(3, 8))
+    order, offsets = rl.scenes.cluster_order(hs.lights, k, 3)
+    lights = np.ascontiguousarray(hs.lights[order])
+    ctx = rl.Context(0)
+    l0, l1, kk = gd.ltc()
+    scene = rl.Scene(ctx, lights, hs.max_vertex_count, l0, l1, kk, hs.triangles)
+    scene.set_clusters(offsets)
+    model = rl.Model(ctx, k, seed=5)
+    params = model.get_params()
+    params[64 * 144 + 64 + 64 * 64 + 64:] *= 10.0  # a non-uniform proposal
+    model.set_params(params)
+    model.set_input_transform((0.0, 0.0, 1.0), 6.0)
+    scene.set_model(model)
+    model.set_training(True, learning_rate=1e-3, pixel_stride=3)  # 5,120 training pixels, 40 tiles
+    model.set_target_mix(0.5)
+    g = torch.from_numpy(np.ascontiguousarray(hs.gbuffer)).cuda()
+    prim = torch.from_numpy(np.ascontiguousarray(hs.primitive).view(np.int32)).cuda()
+    out = torch.zeros((hs.width * hs.height, 3), dtype=torch.float32, device="cuda")
+    s = rl.settings(candidates=32, proposal="learned", proposal_uniform_fraction=0.1)
+    grads = []
+    for cuda_cores in (False, True):
+        model.set_training_flags(cuda_cores=cuda_cores, accumulate_only=True)
+        rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=4, frames=1, out_rgb=out, primitive=prim)
+        grads.append(model.get_gradient(clear=True))
+    ctx.check()
+    assert np.array_equal(model.get_params(), params)
+    tc, ref = grads
+    for name, sl in gradient_blocks(k):
+        scale = np.abs(ref[sl]).max()
+        err = np.abs(tc[sl] - ref[sl]).max()
+        print("k=%d %s: max |g| %.3e, max error %.3e (%.2f%%)" % (k, name, scale, err, 100 * err / scale))
+        assert scale > 0
+        assert err <= 0.05 * scale, name
+    corr = np.corrcoef(tc, ref)[0, 1]
+    print("k=%d correlation %.5f" % (k, corr))
+    assert corr > 0.995
+    # The accumulated gradient drives one Adam step on request.
+    model.set_training_flags(accumulate_only=True)
+    rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=4, frames=1, out_rgb=out, primitive=prim)
+    model.apply_update()
+    moved = model.get_params()
+    assert np.all(model.get_gradient() == 0.0)
+    ctx.check()
+    scene.close()
+    model.close()
+    ctx.close()
+    w3 = slice(64 * 144 + 4224, 64 * 144 + 4224 + 64 * k)
+    assert np.abs(moved[w3] - params[w3]).max() > 0
+    assert np.array_equal(moved[:64 * 144].reshape(64, 144)[:, 130:], params[:64 * 144].reshape(64, 144)[:, 130:])
+
+
+@pytest.mark.gpu
+def test_training_tensor_wait_timeout_is_reported_and_the_context_survives(gpu):
+    """Fault injection on the host for the tensor-core training kernel: it
+    issues no products, its bounded waits run out, it records the timeout,
+    adds nothing to the gradient and frees its tensor memory; the next
+    training call works."""
+    import torch
+    import risltc_gb300 as rl
+    sc, offsets, _, _ = clustered(gd.scene("hf"), 8)
+    ctx = rl.Context(0)
+    l0, l1, k = gd.ltc()
+    scene = rl.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    scene.set_clusters(offsets)
+    model = rl.Model(ctx, 8, seed=5)
+    model.set_input_transform((0.0, 0.0, 1.0), 6.0)
+    scene.set_model(model)
+    model.set_training(True, learning_rate=1e-3, pixel_stride=1)
+    model.set_training_flags(accumulate_only=True)
+    g = torch.from_numpy(np.ascontiguousarray(sc["gbuffer"])).cuda()
+    out = torch.zeros((sc["width"] * sc["height"], 3), dtype=torch.float32, device="cuda")
+    s = rl.settings(candidates=32, proposal="learned", proposal_uniform_fraction=0.1)
+    ctx.inject_fault(train_tensor_wait=True)
+    rl.shade(ctx, scene, g, sc["width"], sc["height"], s, noise_seed=2, frames=1, out_rgb=out)
+    with pytest.raises(rl.RisltcError) as e:
+        ctx.check()
+    assert e.value.status == 11  # RISLTC_ERROR_DEVICE_TIMEOUT
+    assert np.all(model.get_gradient(clear=True) == 0.0)
+    rl.shade(ctx, scene, g, sc["width"], sc["height"], s, noise_seed=2, frames=1, out_rgb=out)
+    ctx.check()
+    assert np.abs(model.get_gradient()).max() > 0
+    scene.close()
+    model.close()
+    ctx.close()
