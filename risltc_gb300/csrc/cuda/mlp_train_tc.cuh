@@ -12,8 +12,8 @@
 // twice.  Per tile:
 //   D1 = E W1^T, H1 = ReLU(D1 + b1); D2 = H1 W2^T, H2 = ReLU(D2 + b2);
 //   logits in chunks of 128 clusters, BF16 into DZ, softmax per pixel;
-//   DZ = (q - T) / B as in the CUDA-core kernel (the target T scattered with
-//   shared-memory BF16 atomics);
+//   DZ = (q - T) / B as in the CUDA-core kernel (each thread subtracts its
+//   own pixel's target T from its row);
 //   dh2 = DZ W3 and dW3 += DZ^T [H2 | 1]; DZ2 = dh2 * [H2 > 0];
 //   dh1 = DZ2 W2 and dW2 += DZ2^T [H1 | 1]; DZ1 = dh1 * [H1 > 0];
 //   dW1 += DZ1^T E (feature 130 of E is 1, so its column is db1).
@@ -80,7 +80,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_train_tc_kernel(MlpT
 	const int chunks = (k_pad + kTcChunk - 1) / kTcChunk;
 	const uint32_t dz_rows = (uint32_t) (k_pad / 8) * 128;  // DZ: bytes between 8-pixel groups
 	const MlpLayout lay = mlp_layout(k_count);
-	const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+	const uint32_t tid = threadIdx.x, warp = tid / 32;
 	const uint32_t base = smem_address(tt_smem);
 	float* b1 = reinterpret_cast<float*>(tt_smem + kTtBias);
 	float* b2 = b1 + kMlpHidden;
@@ -192,24 +192,28 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_train_tc_kernel(MlpT
 	bool accumulated = false;  // the weight gradients in tensor memory hold at least one tile
 	for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
 		const uint32_t j0 = tile * kTcRows;
-		// Encode the tile's training pixels into E; feature 130 is 1.0.
-		for (int idx = tid; idx < kTcRows * kMlpInputs; idx += kTcThreads) {
-			const int r = idx / kMlpInputs, input = idx % kMlpInputs;
-			const uint32_t j = j0 + (uint32_t) r;
-			const bool in = j < n_train;
-			float e[13];
-			mlp_encode(in ? mlp_input(pr.gbuffer, np, pr.phase + j * pr.stride, pr.center, pr.inv_half_extent, input)
-			              : 0.0f,
-			           e);
+		// Thread tid takes the tile's row tid: training pixel j0 + tid.  Its
+		// inputs are loaded together, then encoded into E (feature 130 is 1.0).
+		const uint32_t my_j = j0 + tid, my_i = pr.phase + my_j * pr.stride;
+		const bool in = my_j < n_train;
+		{
+			float x[kMlpInputs];
 #pragma unroll
-			for (int kind = 0; kind != 13; ++kind)
-				*reinterpret_cast<__nv_bfloat16*>(tt_smem + kTtE + tc_offset(r, input * 13 + kind, kMlpFeatures)) =
-				    __float2bfloat16_rn(in ? e[kind] : 0.0f);
-		}
-		for (int idx = tid; idx < kTcRows * (kMlpFeatures - kTtOnesFeature); idx += kTcThreads) {
-			const int r = idx / (kMlpFeatures - kTtOnesFeature), f = kTtOnesFeature + idx % (kMlpFeatures - kTtOnesFeature);
-			*reinterpret_cast<__nv_bfloat16*>(tt_smem + kTtE + tc_offset(r, f, kMlpFeatures)) =
-			    __float2bfloat16_rn(f == kTtOnesFeature ? 1.0f : 0.0f);
+			for (int input = 0; input != kMlpInputs; ++input)
+				x[input] = in ? mlp_input(pr.gbuffer, np, my_i, pr.center, pr.inv_half_extent, input) : 0.0f;
+#pragma unroll
+			for (int input = 0; input != kMlpInputs; ++input) {
+				float e[13];
+				mlp_encode(x[input], e);
+#pragma unroll
+				for (int kind = 0; kind != 13; ++kind)
+					*reinterpret_cast<__nv_bfloat16*>(tt_smem + kTtE + tc_offset((int) tid, input * 13 + kind, kMlpFeatures)) =
+					    __float2bfloat16_rn(in ? e[kind] : 0.0f);
+			}
+#pragma unroll
+			for (int f = kTtOnesFeature; f != kMlpFeatures; ++f)
+				*reinterpret_cast<__nv_bfloat16*>(tt_smem + kTtE + tc_offset((int) tid, f, kMlpFeatures)) =
+				    __float2bfloat16_rn(f == kTtOnesFeature ? 1.0f : 0.0f);
 		}
 		sync_for_products();
 		issue([&] {
@@ -217,23 +221,14 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_train_tc_kernel(MlpT
 				tc_mma(tmem, tc_descriptor(base + kTtE + 256 * k, kMlpFeatures),
 				       tc_descriptor(base + kTtW1 + 256 * k, kMlpFeatures), tc_instruction(kTcRows, kMlpHidden), k > 0);
 		});
-		// While layer 1 runs: each warp sums the candidate weights of its 32
-		// pixels (lane = candidate), lane r keeping row 32 warp + r's total.
+		// While layer 1 runs: the total candidate weight of this thread's pixel.
+		const ProposalCandidate* cand = pr.candidates + (size_t) my_i * mc;
+		const bool valid = in && !(pr.primitive && pr.primitive[my_i] == 0xffffffffu);
 		float total = 0.0f;
-		bool valid = false;
-		for (int rr = 0; rr != 32; ++rr) {
-			const uint32_t j = j0 + warp * 32 + (uint32_t) rr, i = pr.phase + j * pr.stride;
-			const bool v = j < n_train && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
-			float t = 0.0f;
-			if (v)
-				for (int c = (int) lane; c < mc; c += 32) t += pr.candidates[(size_t) i * mc + c].pdf;
-			for (int d = 16; d != 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
-			if ((int) lane == rr) {
-				total = t;
-				valid = v;
-			}
+		if (valid) {
+#pragma unroll 8
+			for (int c = 0; c < mc; ++c) total += cand[c].pdf;
 		}
-		const uint32_t my_i = pr.phase + (j0 + tid) * pr.stride;
 		const bool learn = valid && total > 0.0f && total <= 3.0e38f;
 		const float wu = pr.shaded ? 1.0f - pr.shadowed_weight : 1.0f;
 		float ss = 0.0f;
@@ -313,26 +308,24 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_train_tc_kernel(MlpT
 				o[k] = pack_bf16x2(scale * __expf(bf16_lo(w[k]) - zmax), scale * __expf(bf16_hi(w[k]) - zmax));
 			*p = out;
 		}
-		__syncwarp();
-		// Minus the target: each warp scatters its pixels' candidate weights
-		// into their clusters (lane = candidate), and the shadowed part into
-		// the chosen light's cluster.
-		for (int rr = 0; rr != 32; ++rr) {
-			if (!__shfl_sync(0xffffffffu, learn, rr)) continue;
-			const float t = __shfl_sync(0xffffffffu, total, rr), s = __shfl_sync(0xffffffffu, ss, rr);
-			const int ch = __shfl_sync(0xffffffffu, chosen, rr);
-			const int row = (int) (warp * 32) + rr;
-			const uint32_t i = pr.phase + (j0 + (uint32_t) row) * pr.stride;
-			for (int c = (int) lane; c < mc; c += 32) {
-				const ProposalCandidate q = pr.candidates[(size_t) i * mc + c];
-				if (q.pdf > 0.0f)
-					atomicAdd(reinterpret_cast<__nv_bfloat16*>(tt_smem + kTtDz +
-					                                           tc_offset(row, (int) pr.light_cluster[q.light], k_pad)),
-					          __float2bfloat16_rn(-wu * q.pdf / t * pr.inv_batch));
+		// Minus the target, on this thread's own row: the candidates' weights
+		// into their clusters, the shadowed part into the chosen light's.
+		if (learn) {
+			const float unshadowed = wu / total * pr.inv_batch;
+#pragma unroll 8
+			for (int c = 0; c < mc; ++c) {
+				const ProposalCandidate q = cand[c];
+				if (q.pdf > 0.0f) {
+					__nv_bfloat16* z = reinterpret_cast<__nv_bfloat16*>(
+					    tt_smem + kTtDz + tc_offset((int) tid, (int) pr.light_cluster[q.light], k_pad));
+					*z = __float2bfloat16_rn(__bfloat162float(*z) - unshadowed * q.pdf);
+				}
 			}
-			if (lane == 0 && ch >= 0 && s > 0.0f)
-				atomicAdd(reinterpret_cast<__nv_bfloat16*>(tt_smem + kTtDz + tc_offset(row, (int) pr.light_cluster[ch], k_pad)),
-				          __float2bfloat16_rn(-s * pr.inv_batch));
+			if (chosen >= 0 && ss > 0.0f) {
+				__nv_bfloat16* z = reinterpret_cast<__nv_bfloat16*>(
+				    tt_smem + kTtDz + tc_offset((int) tid, (int) pr.light_cluster[chosen], k_pad));
+				*z = __float2bfloat16_rn(__bfloat162float(*z) - ss * pr.inv_batch);
+			}
 		}
 		sync_for_products();
 		// dh2 = DZ W3 (W3 read MN-major: N = hidden, K = clusters) and
