@@ -74,6 +74,8 @@ def parse():
                    help="equal-mse: the learned proposal's Adam step (measured: 1e-3 trains too slowly in 64 frames, "
                         "5e-3 and 1e-2 equally well)")
     p.add_argument("--train-stride", type=int, default=16, help="equal-mse: every n-th pixel trains the model")
+    p.add_argument("--train-on-cuda-cores", action="store_true",
+                   help="equal-mse: train with the FP32 CUDA-core kernel instead of the tensor cores")
     p.add_argument("--uniform-fraction", type=float, default=0.05,
                    help="equal-mse: weight of uniform light choice in the proposals' defensive mixture (measured on "
                         "960x540: 0.05 gives a lower MSE than 0.1 for both proposals)")
@@ -483,6 +485,7 @@ def run_equal_mse(a):
     ctx.check()
     # Online training of the model (1 spp per call, its own candidates).
     model.set_training(True, learning_rate=a.learning_rate, pixel_stride=a.train_stride)
+    model.set_training_flags(cuda_cores=a.train_on_cuda_cores)
     model.set_target_mix(a.shadowed_target)
     out = torch.empty((P, 3), dtype=torch.float32, device="cuda")
     seed = 20_000_000
@@ -549,6 +552,7 @@ def run_equal_mse(a):
                                               a.candidates, a.spp, a.reference_spp),
                    "train_frames": a.train_frames, "train_ms_per_frame": train_ms, "learning_rate": a.learning_rate,
                    "train_stride": a.train_stride, "uniform_fraction": a.uniform_fraction,
+                   "training": "cuda cores fp32" if a.train_on_cuda_cores or a.clusters > 256 else "tensor cores bf16",
                    "shadowed_target": a.shadowed_target},
         "plain_ms_to_equal_mse": base["ms_to_plain_mse"],
         "speedup_vs_plain": base["ms_to_plain_mse"] / results["learned"]["ms_to_plain_mse"],
