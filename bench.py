@@ -19,6 +19,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -60,6 +61,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--clocks-csv", default=None, help="keep the raw nvidia-smi clock samples in this file")
     p.add_argument("--workload", choices=["throughput", "equal-mse", "batch"], default="throughput",
                    help="equal-mse: device time to equal MSE, learned cluster proposal vs plain RIS; batch: 16 "
                         "plane-of-quads scenes of mixed sizes in one autotuned, graph-captured batched launch")
@@ -102,12 +104,18 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device_index=0):
+    def __init__(self, device_index=0, path=None):
+        """path: where the raw samples go (kept); default a temporary file,
+        removed by stop()."""
         self.proc = None
         self.t0 = self.t1 = None
-        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+        self.keep = path is not None
+        if path is None:
+            fd, path = tempfile.mkstemp(prefix="risltc_clocks_", suffix=".csv")
+            os.close(fd)
+        self.path = path
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(device_index), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
@@ -138,6 +146,8 @@ class ClockSampler:
                 except ValueError:
                     ts = None
                 rows.append((ts, parts[1:]))
+        if not self.keep:
+            os.remove(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         window = [r for ts, r in rows if ts is not None and self.t0 is not None and self.t0 <= ts <= self.t1]
@@ -275,7 +285,7 @@ def run_ours(a, rank, world, local_rank):
     out = torch.empty((P, 3), dtype=torch.float32, device="cuda")
     # Each rank shades different frames (its own noise seeds).
     seed = rank * 1_000_000
-    clocks = ClockSampler(local_rank) if rank == 0 else None
+    clocks = ClockSampler(local_rank, a.clocks_csv) if rank == 0 else None
     for _ in range(a.warmup):
         seed = rl.shade(ctx, scene, g, hs.width, hs.height, s, noise_seed=seed, frames=a.spp, out_rgb=out,
                         primitive=prim)
@@ -618,7 +628,7 @@ def run_batch(a):
             graph.replay()
     torch.cuda.synchronize()
     ctx.check()
-    clocks = ClockSampler(0)
+    clocks = ClockSampler(0, a.clocks_csv)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks.mark_start()
     with torch.cuda.stream(stream):
