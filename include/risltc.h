@@ -195,12 +195,18 @@ EXTERN_C int risltc_ltc_table_synthetic(risltc_ltc_table_t* table, uint64_t seed
                                         uint32_t inclination_count);
 EXTERN_C void risltc_ltc_table_destroy(risltc_ltc_table_t* table);
 
-/* Binary BVH over triangles, built on the host by binned SAH.  Node =
+/* Binary BVH over triangles, built on the host by binned SAH over
+   references: a triangle whose box is large against the mean is cut into up
+   to 8 pieces (early split clipping), each a reference to the whole triangle
+   with the piece's box, at most 3 references per triangle in all.  Node =
    8 x 32-bit words {bmin.xyz, left_or_first, bmax.xyz, count}; count == 0
    marks an interior node with children left and left + 1; a leaf covers
-   triangles [first, first + count) of the reordered triangle array, 12 floats
-   each {v0, 0, v1 - v0, 0, v2 - v0, 0}.  Boxes are widened by a relative
-   1e-6 so that traversal never culls a box that holds a hit. */
+   references [first, first + count) of the reordered triangle array
+   (triangle_count references, 12 floats each {v0, 0, v1 - v0, 0, v2 - v0, 0},
+   triangle_ids[k] the input triangle of reference k).  Every point of a
+   triangle lies in the box of a leaf that references it, and boxes are
+   widened by a relative 1e-6, so traversal never culls a box that holds a
+   hit; any-hit answers equal a brute-force test of every triangle. */
 typedef struct risltc_bvh_s {
 	uint32_t node_count, triangle_count, depth;
 	uint32_t padding;

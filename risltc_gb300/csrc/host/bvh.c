@@ -1,4 +1,5 @@
-/* Binary BVH over occluder triangles, built on the host with a binned SAH.
+/* Binary BVH over occluder triangles, built on the host with a binned SAH
+ * over references made by early split clipping (below).
  *
  * Replaces the driver-built acceleration structure of the reference
  * (create_acceleration_structure, src/scene.c:142-400: one BLAS over all
@@ -14,6 +15,13 @@
 
 #define BVH_BINS 16
 #define BVH_MAX_DEPTH 60
+/* Early split clipping: references per triangle at most, box area (against
+   the mean triangle box) above which a reference is cut, and the references
+   at most, as a multiple of the triangles. */
+#define BVH_SPLIT_PIECES 8
+#define BVH_SPLIT_AREA 0.5f
+#define BVH_SPLIT_BUDGET 3u
+#define BVH_MAX_REFERENCES ((1u << 28) - 1u) /* leaf references keep 28 bits for the first index */
 
 typedef struct {
 	float lo[3], hi[3];
@@ -47,19 +55,120 @@ typedef struct {
 	uint32_t node, begin, end, depth;
 } task_t;
 
+/* Early split clipping (Ernst and Greiner, "Early split clipping for bounding
+   volume hierarchies", 2007): a triangle whose box area is more than
+   BVH_SPLIT_AREA times the mean is cut at the middle of its largest piece's
+   longest box axis (the piece, a convex polygon, clipped against the plane
+   on both sides) until every piece's box is small enough, it has
+   BVH_SPLIT_PIECES pieces, or `room` references are used.  Each piece is a
+   reference to the whole triangle with the piece's box.  The pieces cover the
+   triangle, so a ray that hits it passes through one piece's box, reaches
+   that leaf and tests the triangle: any-hit answers do not change (the node
+   boxes' widening covers the rounding of the cut points).  Returns the
+   number of references written. */
+static uint32_t split_triangle(const float* tri, const box_t* box, float limit, uint32_t room, uint32_t id,
+                               box_t* ref_box, uint32_t* ref_tri) {
+	enum { kMaxVertices = 3 + BVH_SPLIT_PIECES };
+	float poly[BVH_SPLIT_PIECES][kMaxVertices][3];
+	int vertices[BVH_SPLIT_PIECES];
+	box_t pbox[BVH_SPLIT_PIECES];
+	uint32_t pieces = 1;
+	for (int v = 0; v != 3; ++v)
+		for (int a = 0; a != 3; ++a) poly[0][v][a] = tri[3 * v + a];
+	vertices[0] = 3;
+	pbox[0] = *box;
+	if (room > BVH_SPLIT_PIECES) room = BVH_SPLIT_PIECES;
+	while (pieces < room) {
+		int k = -1;
+		float largest = limit;
+		for (uint32_t j = 0; j != pieces; ++j)
+			if (box_area(&pbox[j]) > largest) {
+				largest = box_area(&pbox[j]);
+				k = (int) j;
+			}
+		if (k < 0) break;
+		int ax = 0;
+		for (int a = 1; a != 3; ++a)
+			if (pbox[k].hi[a] - pbox[k].lo[a] > pbox[k].hi[ax] - pbox[k].lo[ax]) ax = a;
+		const float mid = 0.5f * (pbox[k].lo[ax] + pbox[k].hi[ax]);
+		float lo_side[kMaxVertices][3], hi_side[kMaxVertices][3];
+		int nl = 0, nh = 0;
+		const int n = vertices[k];
+		for (int v = 0; v != n; ++v) {
+			const float* p = poly[k][v];
+			const float* q = poly[k][(v + 1) % n];
+			const int p_lo = p[ax] <= mid, q_lo = q[ax] <= mid;
+			if (p_lo)
+				memcpy(lo_side[nl++], p, sizeof(float) * 3);
+			else
+				memcpy(hi_side[nh++], p, sizeof(float) * 3);
+			if (p_lo != q_lo) {
+				/* The edge crosses the plane: the cut point goes to both sides. */
+				const float t = (mid - p[ax]) / (q[ax] - p[ax]);
+				float x[3];
+				for (int a = 0; a != 3; ++a) x[a] = p[a] + t * (q[a] - p[a]);
+				x[ax] = mid;
+				memcpy(lo_side[nl++], x, sizeof(x));
+				memcpy(hi_side[nh++], x, sizeof(x));
+			}
+		}
+		if (nl < 3 || nh < 3) break; /* the plane does not cut this piece */
+		memcpy(poly[k], lo_side, sizeof(float) * 3 * (size_t) nl);
+		memcpy(poly[pieces], hi_side, sizeof(float) * 3 * (size_t) nh);
+		vertices[k] = nl;
+		vertices[pieces] = nh;
+		box_empty(&pbox[k]);
+		for (int v = 0; v != nl; ++v) box_grow_point(&pbox[k], lo_side[v]);
+		box_empty(&pbox[pieces]);
+		for (int v = 0; v != nh; ++v) box_grow_point(&pbox[pieces], hi_side[v]);
+		++pieces;
+	}
+	for (uint32_t j = 0; j != pieces; ++j) {
+		ref_box[j] = pbox[j];
+		ref_tri[j] = id;
+	}
+	return pieces;
+}
+
 int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint32_t max_leaf_size) {
 	if (!bvh || (!tris && count)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	memset(bvh, 0, sizeof(*bvh));
 	if (count == 0) return RISLTC_OK;
 	if (max_leaf_size < 1) max_leaf_size = 4;
-	box_t* boxes = (box_t*) malloc(sizeof(box_t) * count);
+	if (count > BVH_MAX_REFERENCES) return RISLTC_ERROR_INVALID_ARGUMENT;
+	const uint32_t triangle_count = count;
+	uint32_t room = count <= BVH_MAX_REFERENCES / BVH_SPLIT_BUDGET ? count * BVH_SPLIT_BUDGET : BVH_MAX_REFERENCES;
+	box_t* tri_box = (box_t*) malloc(sizeof(box_t) * count);
+	box_t* boxes = (box_t*) malloc(sizeof(box_t) * room);
+	uint32_t* ref_tri = (uint32_t*) malloc(sizeof(uint32_t) * room);
+	if (!tri_box || !boxes || !ref_tri) {
+		free(tri_box);
+		free(boxes);
+		free(ref_tri);
+		return RISLTC_ERROR_OUT_OF_MEMORY;
+	}
+	double mean_area = 0.0;
+	for (uint32_t i = 0; i != count; ++i) {
+		box_empty(&tri_box[i]);
+		for (int v = 0; v != 3; ++v) box_grow_point(&tri_box[i], tris + 9 * (size_t) i + 3 * v);
+		mean_area += box_area(&tri_box[i]);
+	}
+	const float limit = (float) (BVH_SPLIT_AREA * mean_area / count);
+	count = 0;
+	for (uint32_t i = 0; i != triangle_count; ++i) {
+		/* Leave one reference for each triangle still to come. */
+		const uint32_t left = room - count - (triangle_count - 1 - i);
+		count += split_triangle(tris + 9 * (size_t) i, &tri_box[i], limit, left, i, boxes + count, ref_tri + count);
+	}
+	free(tri_box);
 	float* centroid = (float*) malloc(sizeof(float) * 3 * count);
 	uint32_t* ids = (uint32_t*) malloc(sizeof(uint32_t) * count);
 	uint32_t capacity = 2 * count;
-	float* nodes = (float*) malloc(sizeof(float) * 8 * capacity);
+	float* nodes = (float*) malloc(sizeof(float) * 8 * (size_t) capacity);
 	task_t* stack = (task_t*) malloc(sizeof(task_t) * (BVH_MAX_DEPTH + 4) * 2);
-	if (!boxes || !centroid || !ids || !nodes || !stack) {
+	if (!centroid || !ids || !nodes || !stack) {
 		free(boxes);
+		free(ref_tri);
 		free(centroid);
 		free(ids);
 		free(nodes);
@@ -67,8 +176,6 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 		return RISLTC_ERROR_OUT_OF_MEMORY;
 	}
 	for (uint32_t i = 0; i != count; ++i) {
-		box_empty(&boxes[i]);
-		for (int v = 0; v != 3; ++v) box_grow_point(&boxes[i], tris + 9 * (size_t) i + 3 * v);
 		for (int a = 0; a != 3; ++a) centroid[3 * i + a] = 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]);
 		ids[i] = i;
 	}
@@ -192,6 +299,8 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 	bvh->node_count = node_count;
 	bvh->depth = max_depth;
 	bvh->triangle_count = count;
+	for (uint32_t i = 0; i != count; ++i) ids[i] = ref_tri[ids[i]];
+	free(ref_tri);
 	bvh->triangle_ids = ids;
 	bvh->triangles = (float*) malloc(sizeof(float) * 12 * (size_t) count);
 	if (!bvh->triangles) {

@@ -174,17 +174,24 @@ def test_synthetic_ltc_table_is_valid():
 
 
 def test_bvh_invariants():
+    """Nested boxes; every reference in exactly one leaf; every triangle
+    referenced at least once (large ones cut into pieces, at most three
+    references per triangle in all); and conservative leaves: points all over
+    each triangle lie in the box of a leaf that references it, so a ray that
+    hits a triangle reaches a leaf that tests it."""
     from risltc_gb300 import api, scenes
     rng = np.random.default_rng(0)
     tris = scenes.random_triangles(rng, 5000)
     nodes, reordered, ids, depth = api.build_bvh(tris)
-    assert sorted(ids.tolist()) == list(range(5000))
+    assert set(ids.tolist()) == set(range(5000))
+    assert 5000 < len(ids) <= 3 * 5000
     assert depth <= 60
     words = nodes.view(np.int32)
     v0 = tris.reshape(-1, 3, 3)[ids]
     assert np.array_equal(reordered[:, 0:3], v0[:, 0])
     assert np.array_equal(reordered[:, 4:7], v0[:, 1] - v0[:, 0])
-    covered = np.zeros(5000, int)
+    covered = np.zeros(len(ids), int)
+    leaf_boxes = {}
 
     def visit(i, lo, hi):
         n = nodes[i]
@@ -197,11 +204,19 @@ def test_bvh_invariants():
         else:
             for k in range(first, first + count):
                 covered[k] += 1
-                t = v0[k]
-                assert (t >= n[0:3]).all() and (t <= n[4:7]).all()
+                leaf_boxes.setdefault(int(ids[k]), []).append((n[0:3], n[4:7]))
 
     import sys
     sys.setrecursionlimit(10000)
     visit(0, nodes[0, 0:3], nodes[0, 4:7])
     assert (covered == 1).all()
+    t = tris.reshape(-1, 3, 3).astype(np.float64)
+    bary = np.concatenate([np.eye(3), [[0.5, 0.5, 0], [0, 0.5, 0.5], [0.5, 0, 0.5], [1 / 3, 1 / 3, 1 / 3]],
+                           rng.dirichlet([1, 1, 1], 24)])
+    for tri in range(5000):
+        pts = (bary @ t[tri]).astype(np.float32)
+        inside = np.zeros(len(pts), bool)
+        for lo, hi in leaf_boxes[tri]:
+            inside |= ((pts >= lo) & (pts <= hi)).all(axis=1)
+        assert inside.all(), tri
     assert api.build_bvh(np.zeros((0, 9), np.float32))[0].shape == (0, 8)
