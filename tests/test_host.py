@@ -220,3 +220,43 @@ def test_bvh_invariants():
             inside |= ((pts >= lo) & (pts <= hi)).all(axis=1)
         assert inside.all(), tri
     assert api.build_bvh(np.zeros((0, 9), np.float32))[0].shape == (0, 8)
+
+
+@pytest.mark.parametrize("kind", ["small", "large", "mixed"])
+def test_bvh_shadow_answers_equal_brute_force(kind):
+    """The oracle's frame with shadow rays traced through the product's BVH
+    (split-clipped references) equals the same frame with every triangle
+    tested, pixel for pixel: small occluders, large ones (cut into pieces),
+    and a mix with degenerate and axis-aligned triangles."""
+    import oracle
+    from risltc_gb300 import api, scenes
+    hs = scenes.heightfield(96, 54, light_count=24, triangle_count=0, seed=3)
+    rng = np.random.default_rng(11)
+    small = scenes.random_triangles(rng, 1500)
+    large = scenes.random_triangles(rng, 300, edge=(1.0, 4.0))
+    if kind == "small":
+        tris = small
+    elif kind == "large":
+        tris = large
+    else:
+        flat = scenes.random_triangles(rng, 200, edge=(0.5, 3.0)).reshape(-1, 3, 3)
+        flat[:, :, 2] = 1.0  # axis-aligned: all in the plane z = 1
+        degenerate = scenes.random_triangles(rng, 50).reshape(-1, 3, 3)
+        degenerate[:, 2] = degenerate[:, 1]
+        tris = np.concatenate([small.reshape(-1, 9), large.reshape(-1, 9), flat.reshape(-1, 9),
+                               degenerate.reshape(-1, 9)]).astype(np.float32)
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    nodes, refs, ids, _ = api.build_bvh(tris)
+    if kind != "small":
+        assert len(ids) > len(tris)
+    st = oracle.make_settings(candidates=8)
+    rn = api.noise_constants(5)[0]
+    through = oracle.OracleScene(hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants, refs, nodes)
+    brute = oracle.OracleScene(hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants,
+                               oracle.triangles_v0e1e2(tris))
+    a, _, _ = oracle.render(through, st, hs.gbuffer, hs.width, hs.height, rn, reservoirs=False)
+    b, _, _ = oracle.render(brute, st, hs.gbuffer, hs.width, hs.height, rn, reservoirs=False)
+    assert np.array_equal(a, b)
+    unshadowed = oracle.OracleScene(hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants)
+    c, _, _ = oracle.render(unshadowed, st, hs.gbuffer, hs.width, hs.height, rn, reservoirs=False)
+    assert not np.array_equal(a, c)  # the occluders do shadow the frame
