@@ -27,19 +27,30 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
+def count_name(n):
+    """200000 -> '200k'; counts that are not whole thousands as they are."""
+    return "%dk" % (n // 1000) if n >= 1000 and n % 1000 == 0 else str(n)
+
+
 def workload_name(a):
     if a.scene == "plane":
         return ("plane of quads: %dx%d G-buffer on z = 0, %d quad lights, %s, plain LTC-RIS M=%d, %d spp"
-                % (a.width, a.height, a.lights, "%dk occluder triangles" % (a.triangles // 1000) if a.triangles
+                % (a.width, a.height, a.lights, "%s occluder triangles" % count_name(a.triangles) if a.triangles
                    else "unshadowed", a.candidates, a.spp))
-    return ("shadowed single frame: %dx%d fBm heightfield, %d polygon lights (3-8 vertices), %dk occluder "
-            "triangles (SAH BVH), plain LTC-RIS M=%d, %d spp" % (a.width, a.height, a.lights, a.triangles // 1000,
-                                                                 a.candidates, a.spp))
+    return ("shadowed single frame: %dx%d fBm heightfield, %d polygon lights (3-8 vertices), %s occluder "
+            "triangles (SAH BVH), plain LTC-RIS M=%d, %d spp" % (a.width, a.height, a.lights,
+                                                                count_name(a.triangles), a.candidates, a.spp))
 METRIC = "Gsamples/s (plain LTC-RIS, shadowed 1080p frame, 1024 lights, M=32, 4 spp)"
 
 
 def metric_name(a):
-    return METRIC if a.scene == "heightfield" else "Gsamples/s (%s)" % workload_name(a)
+    """The headline metric's name for its own workload (1080p heightfield,
+    1024 lights, 200k occluders, M = 32, 4 spp), else one naming the workload."""
+    headline = (a.scene == "heightfield" and (a.width, a.height, a.lights, a.triangles, a.candidates, a.spp)
+                == (1920, 1080, 1024, 200_000, 32, 4))
+    return METRIC if headline else "Gsamples/s (%s)" % workload_name(a)
+
+
 L2_BYTES = 129 * 1024 * 1024
 
 
