@@ -161,24 +161,23 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 		count += split_triangle(tris + 9 * (size_t) i, &tri_box[i], limit, left, i, boxes + count, ref_tri + count);
 	}
 	free(tri_box);
+	/* The references (box, centroid, triangle) are reordered in place as the
+	   build partitions them, so every pass over a node's range reads them in
+	   sequence. */
 	float* centroid = (float*) malloc(sizeof(float) * 3 * count);
-	uint32_t* ids = (uint32_t*) malloc(sizeof(uint32_t) * count);
 	uint32_t capacity = 2 * count;
 	float* nodes = (float*) malloc(sizeof(float) * 8 * (size_t) capacity);
 	task_t* stack = (task_t*) malloc(sizeof(task_t) * (BVH_MAX_DEPTH + 4) * 2);
-	if (!centroid || !ids || !nodes || !stack) {
+	if (!centroid || !nodes || !stack) {
 		free(boxes);
 		free(ref_tri);
 		free(centroid);
-		free(ids);
 		free(nodes);
 		free(stack);
 		return RISLTC_ERROR_OUT_OF_MEMORY;
 	}
-	for (uint32_t i = 0; i != count; ++i) {
+	for (uint32_t i = 0; i != count; ++i)
 		for (int a = 0; a != 3; ++a) centroid[3 * i + a] = 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]);
-		ids[i] = i;
-	}
 	uint32_t node_count = 1, max_depth = 0;
 	int sp = 0;
 	stack[sp++] = (task_t){0, 0, count, 0};
@@ -189,8 +188,8 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 		box_empty(&bounds);
 		box_empty(&cbounds);
 		for (uint32_t i = t.begin; i != t.end; ++i) {
-			box_grow_box(&bounds, &boxes[ids[i]]);
-			box_grow_point(&cbounds, centroid + 3 * ids[i]);
+			box_grow_box(&bounds, &boxes[i]);
+			box_grow_point(&cbounds, centroid + 3 * (size_t) i);
 		}
 		float* node = nodes + 8 * (size_t) t.node;
 		/* Widen by a relative 1e-6 so traversal is conservative. */
@@ -217,10 +216,10 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 					bin_count[b] = 0;
 				}
 				for (uint32_t i = t.begin; i != t.end; ++i) {
-					int b = (int) ((centroid[3 * ids[i] + a] - lo) * scale);
+					int b = (int) ((centroid[3 * (size_t) i + a] - lo) * scale);
 					b = b < 0 ? 0 : (b >= BVH_BINS ? BVH_BINS - 1 : b);
 					bin_count[b]++;
-					box_grow_box(&bin_box[b], &boxes[ids[i]]);
+					box_grow_box(&bin_box[b], &boxes[i]);
 				}
 				float right_area[BVH_BINS];
 				uint32_t right_count[BVH_BINS];
@@ -261,14 +260,23 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 			float scale = (float) BVH_BINS / (hi - lo);
 			uint32_t i = t.begin, j = t.end;
 			while (i < j) {
-				int b = (int) ((centroid[3 * ids[i] + split_axis] - lo) * scale);
+				int b = (int) ((centroid[3 * (size_t) i + split_axis] - lo) * scale);
 				b = b < 0 ? 0 : (b >= BVH_BINS ? BVH_BINS - 1 : b);
 				if ((uint32_t) b <= split_bin) {
 					++i;
 				} else {
-					uint32_t tmp = ids[i];
-					ids[i] = ids[--j];
-					ids[j] = tmp;
+					--j;
+					const box_t box = boxes[i];
+					boxes[i] = boxes[j];
+					boxes[j] = box;
+					for (int a = 0; a != 3; ++a) {
+						const float c = centroid[3 * (size_t) i + a];
+						centroid[3 * (size_t) i + a] = centroid[3 * (size_t) j + a];
+						centroid[3 * (size_t) j + a] = c;
+					}
+					const uint32_t tri = ref_tri[i];
+					ref_tri[i] = ref_tri[j];
+					ref_tri[j] = tri;
 				}
 			}
 			mid = i;
@@ -299,9 +307,8 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 	bvh->node_count = node_count;
 	bvh->depth = max_depth;
 	bvh->triangle_count = count;
-	for (uint32_t i = 0; i != count; ++i) ids[i] = ref_tri[ids[i]];
-	free(ref_tri);
-	bvh->triangle_ids = ids;
+	uint32_t* ids = (uint32_t*) realloc(ref_tri, sizeof(uint32_t) * count);
+	bvh->triangle_ids = ids ? ids : ref_tri;
 	bvh->triangles = (float*) malloc(sizeof(float) * 12 * (size_t) count);
 	if (!bvh->triangles) {
 		free(boxes);
@@ -311,7 +318,7 @@ int risltc_bvh_build(risltc_bvh_t* bvh, const float* tris, uint32_t count, uint3
 		return RISLTC_ERROR_OUT_OF_MEMORY;
 	}
 	for (uint32_t i = 0; i != count; ++i) {
-		const float* t = tris + 9 * (size_t) ids[i];
+		const float* t = tris + 9 * (size_t) bvh->triangle_ids[i];
 		float* o = bvh->triangles + 12 * (size_t) i;
 		for (int a = 0; a != 3; ++a) {
 			o[a] = t[a];
