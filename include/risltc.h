@@ -541,11 +541,14 @@ EXTERN_C int risltc_shade_host(risltc_ctx_t* ctx, const risltc_scene_t* scene, u
  * which every GPU that loads the library holds until the process exits.
  * width * height * frame_count above that limit returns
  * RISLTC_ERROR_TOO_LARGE before any work.  The call waits for its stream to
- * finish and returns the kernels' error status.  The first call on each
- * device resolves the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU (other streams, other threads) race, so serialise
- * them. */
+ * finish and returns the kernels' error status.  The scene must have been
+ * created on the current device; a scene of another device returns
+ * RISLTC_ERROR_INVALID_ARGUMENT before any work.  The first call on each
+ * device resolves the array's device address (cudaGetSymbolAddress) and keeps
+ * it for the life of the process; make that first call before any stream
+ * capture, and make no call on a device after resetting it
+ * (cudaDeviceReset).  All calls share the array: calls that overlap on the
+ * GPU (other streams, other threads) race, so serialise them. */
 #define RISLTC_NOALLOC_MAX_PIXEL_FRAMES 262144
 EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
                                   const risltc_settings_t* settings, noise_table_t* noise, uint32_t animate,

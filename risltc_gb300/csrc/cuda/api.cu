@@ -405,6 +405,14 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 // The device view of a scene, for the allocation-free entry point (noalloc.cu).
 risltc::SceneView risltc_scene_view(const risltc_scene_t* scene) { return scene->view; }
 
+// The device ordinal whose memory holds the scene's buffers (the ordinal its
+// context was created with).
+int risltc_scene_device_ordinal(const risltc_scene_t* scene) { return scene->ctx->device; }
+// A test fakes a scene's device ordinal through these two offsets (the
+// context pointer first in the scene, the ordinal first in the context).
+static_assert(offsetof(risltc_scene_s, ctx) == 0, "scene layout");
+static_assert(offsetof(risltc_ctx_s, device) == 0, "context layout");
+
 EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene) {
 	if (!scene) return;
 	cudaSetDevice(scene->ctx->device);

@@ -10,11 +10,13 @@
 // synchronise the device).  Such a caller creates the scene once, where
 // allocation is allowed, and then shades every frame through this entry
 // point, which allocates nothing.
+#include <atomic>
 #include <cstring>
 #include <cuda_runtime.h>
 #include "ris_kernels.cuh"
 
 risltc::SceneView risltc_scene_view(const risltc_scene_t* scene);
+int risltc_scene_device_ordinal(const risltc_scene_t* scene);
 
 
 // The scratch: reservoir records for up to RISLTC_NOALLOC_MAX_PIXEL_FRAMES
@@ -30,8 +32,10 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 // Device address of g_noalloc_scratch per device ordinal, resolved on the
-// first call made with that device current.
-NoallocScratch* g_scratch_address[kMaxDevices];
+// first call made with that device current.  Host threads that make their
+// first calls at the same time each resolve the same address and store it;
+// the slots are atomic so that those stores do not race.
+std::atomic<NoallocScratch*> g_scratch_address[kMaxDevices];
 
 int to_status(cudaError_t e) {
 	if (e == cudaSuccess) return RISLTC_OK;
@@ -62,13 +66,17 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 	cudaError_t e = cudaGetDevice(&device);
 	if (e != cudaSuccess) return to_status(e);
 	if (device < 0 || device >= kMaxDevices) return RISLTC_ERROR_UNSUPPORTED;
-	if (!g_scratch_address[device]) {
+	// The scene's buffers must be in the current device's memory: the
+	// kernels run there and read them.
+	if (risltc_scene_device_ordinal(scene) != device) return RISLTC_ERROR_INVALID_ARGUMENT;
+	NoallocScratch* scratch = g_scratch_address[device].load(std::memory_order_relaxed);
+	if (!scratch) {
 		void* address = nullptr;
 		e = cudaGetSymbolAddress(&address, g_noalloc_scratch);
 		if (e != cudaSuccess) return to_status(e);
-		g_scratch_address[device] = (NoallocScratch*) address;
+		scratch = (NoallocScratch*) address;
+		g_scratch_address[device].store(scratch, std::memory_order_relaxed);
 	}
-	NoallocScratch* scratch = g_scratch_address[device];
 	cudaStream_t s = (cudaStream_t) stream;
 	// The records are written in full before they are read; only the error
 	// word has to start at zero.
@@ -96,7 +104,9 @@ EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuf
 	r.reservoirs = reservoirs;
 	r.error = &scratch->error;
 	int sms = 0;
-	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	if (e != cudaSuccess) return to_status(e);
+	if (sms < 1) return RISLTC_ERROR_CUDA;
 	size_t blocks = ((size_t) gbuffer->width * gbuffer->height + 127) / 128;
 	if (blocks > (size_t) sms * 16) blocks = (size_t) sms * 16;
 	// No p_hat scratch: the candidate kernel with one thread per pixel.

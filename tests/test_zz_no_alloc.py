@@ -20,6 +20,7 @@ pytestmark = pytest.mark.gpu
 
 MAX_PIXEL_FRAMES = 262144  # RISLTC_NOALLOC_MAX_PIXEL_FRAMES in include/risltc.h
 TOO_LARGE = 10             # RISLTC_ERROR_TOO_LARGE
+INVALID_ARGUMENT = 1       # RISLTC_ERROR_INVALID_ARGUMENT
 
 
 def test_noalloc_matches_shade_on_two_calls_in_a_row(gpu):
@@ -62,6 +63,15 @@ def test_noalloc_matches_shade_on_two_calls_in_a_row(gpu):
         # parity tests for exact numerics).
         assert torch.equal(got, want), "call %d" % call
         assert torch.equal(got_res, want_res), "call %d" % call
+        if frames == 1:
+            # The same frame from the oracle (the reference's routines in C99).
+            import oracle
+            tris = oracle.triangles_v0e1e2(sc["triangles"])
+            osc = oracle.OracleScene(sc["lights"], sc["max_vertex_count"], l0, l1, k, tris)
+            orgb, _, _ = oracle.render(osc, oracle.make_settings(candidates=c["candidates"]), sc["gbuffer"],
+                                       sc["width"], sc["height"], rl.noise_constants(seed)[0],
+                                       primitive=sc["primitive"])
+            assert np.array_equal(got.cpu().numpy(), orgb), "call %d against the oracle" % call
     # Frames beyond the static scratch are rejected before any launch.
     big = _native.GBuffer(1024, 512, g.data_ptr(), None)
     nt = _native.NoiseTable(0)
@@ -69,5 +79,18 @@ def test_noalloc_matches_shade_on_two_calls_in_a_row(gpu):
     assert lib.risltc_shade_noalloc(scene.handle, ctypes.byref(big), ctypes.byref(s), ctypes.byref(nt), 1, 1,
                                     ctypes.c_void_p(got.data_ptr()), None, None, ctypes.c_void_p(stream)) == TOO_LARGE
     assert nt.random_seed == 0
+    # A scene whose buffers live on another device is rejected before any
+    # launch.  With one GPU the other device is faked: the scene's context
+    # records its device ordinal first, and the scene points to its context
+    # first (static_asserts in api.cu keep that layout).
+    ordinal = ctypes.cast(ctypes.cast(scene.handle, ctypes.POINTER(ctypes.c_void_p))[0], ctypes.POINTER(ctypes.c_int))
+    assert ordinal[0] == 0
+    ordinal[0] = 1
+    try:
+        st = lib.risltc_shade_noalloc(scene.handle, ctypes.byref(gb), ctypes.byref(s), ctypes.byref(nt), 1, 1,
+                                      ctypes.c_void_p(got.data_ptr()), None, None, ctypes.c_void_p(stream))
+    finally:
+        ordinal[0] = 0
+    assert st == INVALID_ARGUMENT and nt.random_seed == 0
     scene.close()
     ctx.close()
