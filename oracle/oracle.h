@@ -20,6 +20,7 @@
  */
 #ifndef RISLTC_ORACLE_H
 #define RISLTC_ORACLE_H
+#include <stddef.h>
 #include <stdint.h>
 
 /* Values of sample_polygon_technique_t (polygonal_light.h:31-46),
@@ -94,6 +95,9 @@ extern "C" {
 #endif
 int oracle_render_f32(const oracle_scene_t*, const oracle_settings_t*, const oracle_gbuffer_t*, uint32_t random_number_x,
                       int row_begin, int row_end, float* out_rgb, oracle_reservoir_t* out_reservoirs);
+int oracle_render_pixels_f32(const oracle_scene_t*, const oracle_settings_t*, const oracle_gbuffer_t*,
+                             uint32_t random_number_x, const uint32_t* pixels, size_t begin, size_t end, float* out_rgb,
+                             oracle_reservoir_t* out_reservoirs);
 int oracle_render_f64(const oracle_scene_t*, const oracle_settings_t*, const oracle_gbuffer_t*, uint32_t random_number_x,
                       int row_begin, int row_end, double* out_rgb, oracle_reservoir_t* out_reservoirs);
 #ifdef __cplusplus

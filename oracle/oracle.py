@@ -65,6 +65,9 @@ def load():
         lib.oracle_render_frame_f32.argtypes = args[:4] + [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                           ctypes.c_void_p, ctypes.c_void_p,
                                                           ctypes.POINTER(ctypes.c_double)]
+        lib.oracle_render_pixels_omp_f32.argtypes = args[:4] + [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                                ctypes.c_void_p, ctypes.c_void_p,
+                                                                ctypes.POINTER(ctypes.c_double)]
         lib.oracle_max_threads.restype = ctypes.c_int
         _lib = lib
     return _lib
@@ -165,6 +168,32 @@ def render(scene, settings, gbuffer, width, height, random_number_x, primitive=N
     else:
         status = lib.oracle_render_f64(ctypes.byref(scene.struct), ctypes.byref(settings), ctypes.byref(g),
                                        random_number_x, r0, r1, rgb.ctypes.data, res_ptr)
+    if status != 0:
+        raise RuntimeError("oracle render failed (status %d)" % status)
+    return rgb, res, seconds.value
+
+
+def render_pixels(scene, settings, gbuffer, width, height, random_number_x, pixels, primitive=None, threads=0,
+                  reservoirs=True):
+    """Renders the listed pixels (indices y * width + x) of a full frame, each
+    with its own position's noise seed, in FP32.  Returns (rgb [K, 3],
+    reservoirs [K] or None, seconds): row k belongs to pixels[k]."""
+    lib = load()
+    g = GBuffer()
+    g.width, g.height = width, height
+    gbuffer = np.ascontiguousarray(gbuffer, np.float32)
+    assert gbuffer.shape == (17, width * height)
+    g.planes = gbuffer.ctypes.data
+    prim = None if primitive is None else np.ascontiguousarray(primitive, np.uint32)
+    g.primitive = None if prim is None else prim.ctypes.data
+    px = np.ascontiguousarray(pixels, np.uint32)
+    assert px.size == 0 or int(px.max()) < width * height
+    rgb = np.zeros((px.size, 3), np.float32)
+    res = np.zeros(px.size, RESERVOIR_DTYPE) if reservoirs else None
+    seconds = ctypes.c_double(0.0)
+    status = lib.oracle_render_pixels_omp_f32(ctypes.byref(scene.struct), ctypes.byref(settings), ctypes.byref(g),
+                                              random_number_x, px.ctypes.data, int(px.size), threads, rgb.ctypes.data,
+                                              None if res is None else res.ctypes.data, ctypes.byref(seconds))
     if status != 0:
         raise RuntimeError("oracle render failed (status %d)" % status)
     return rgb, res, seconds.value

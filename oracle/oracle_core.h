@@ -1269,56 +1269,88 @@ static void shade_pixel(const ctx_t* c, const shading_data_t* sd, uint32_t seed,
 	out_rgb[2] = final_color.z;
 }
 
+/* Shades pixel i = y * width + x of the G-buffer (its own noise seed from
+   x, y and the frame's random number, noise_utility.glsl:77-84), writing its
+   colour to out_rgb[0..2] and, if res is not NULL, its reservoir. */
+static void render_pixel(const ctx_t* c, const oracle_gbuffer_t* gbuffer, uint32_t random_number_x, size_t i,
+                         ORACLE_OUT_T* out_rgb, oracle_reservoir_t* res) {
+	const oracle_scene_t* scene = c->scene;
+	const oracle_settings_t* settings = c->settings;
+	const size_t np = (size_t) gbuffer->width * gbuffer->height;
+	const float* g = gbuffer->planes;
+	const uint32_t x = (uint32_t) (i % (size_t) gbuffer->width), y = (uint32_t) (i / (size_t) gbuffer->width);
+	R rgb[3] = {RC(0.0), RC(0.0), RC(0.0)};
+	if (gbuffer->primitive && gbuffer->primitive[i] == 0xffffffffu) {
+		if (res) {
+			res->light_index = -1;
+			res->w_sum = 0.0;
+			res->sample_value = 0.0;
+		}
+	} else {
+		shading_data_t sd;
+		sd.position = V3((R) g[0 * np + i], (R) g[1 * np + i], (R) g[2 * np + i]);
+		sd.normal = V3((R) g[3 * np + i], (R) g[4 * np + i], (R) g[5 * np + i]);
+		sd.outgoing = V3((R) g[6 * np + i], (R) g[7 * np + i], (R) g[8 * np + i]);
+		sd.lambert_outgoing = (R) g[9 * np + i];
+		sd.diffuse_albedo = V3((R) g[10 * np + i], (R) g[11 * np + i], (R) g[12 * np + i]);
+		sd.fresnel_0 = V3((R) g[13 * np + i], (R) g[14 * np + i], (R) g[15 * np + i]);
+		sd.roughness = (R) g[16 * np + i];
+		uint32_t seed = get_noise_accessor(x, y, (uint32_t) gbuffer->width, random_number_x);
+		proposal_candidate_t candidates[OR_MAX_CANDIDATES];
+		const int proposal = settings->proposal && settings->light_sampling == ORACLE_LIGHT_RESERVOIR &&
+		                     scene->cluster_count > 0 && settings->candidate_count <= OR_MAX_CANDIDATES;
+		if (proposal) {
+			const float xp[3] = {g[0 * np + i], g[1 * np + i], g[2 * np + i]};
+			const float nn[3] = {g[3 * np + i], g[4 * np + i], g[5 * np + i]};
+			proposal_draw(scene, settings, xp, nn, x, y, (uint32_t) gbuffer->width, candidates);
+		}
+		shade_pixel(c, &sd, seed, rgb, res, proposal ? candidates : NULL);
+	}
+	out_rgb[0] = (ORACLE_OUT_T) rgb[0];
+	out_rgb[1] = (ORACLE_OUT_T) rgb[1];
+	out_rgb[2] = (ORACLE_OUT_T) rgb[2];
+}
+
+static int make_ctx(ctx_t* c, const oracle_scene_t* scene, const oracle_settings_t* settings) {
+	c->scene = scene;
+	c->settings = settings;
+	c->maxv = (uint32_t) scene->max_light_vertex_count;
+	c->maxp = c->maxv + 1;
+	if (c->maxv < 3 || c->maxv > OR_MAXV || scene->light_count <= 0) return 1;
+	g_oracle_fast_atan = settings->fast_atan;
+	g_oracle_biased_psa = settings->polygon_sampling_technique == ORACLE_TECHNIQUE_PSA_BIASED;
+	return 0;
+}
+
 /* Renders rows [row_begin, row_end) of one frame. */
 int OR_EXPORT(oracle_render)(const oracle_scene_t* scene, const oracle_settings_t* settings,
                              const oracle_gbuffer_t* gbuffer, uint32_t random_number_x, int row_begin, int row_end,
                              ORACLE_OUT_T* out_rgb, oracle_reservoir_t* out_reservoirs) {
 	ctx_t c;
-	c.scene = scene;
-	c.settings = settings;
-	c.maxv = (uint32_t) scene->max_light_vertex_count;
-	c.maxp = c.maxv + 1;
-	if (c.maxv < 3 || c.maxv > OR_MAXV || scene->light_count <= 0) return 1;
-	g_oracle_fast_atan = settings->fast_atan;
-	g_oracle_biased_psa = settings->polygon_sampling_technique == ORACLE_TECHNIQUE_PSA_BIASED;
-	size_t np = (size_t) gbuffer->width * gbuffer->height;
-	const float* g = gbuffer->planes;
+	if (make_ctx(&c, scene, settings)) return 1;
 	for (int y = row_begin; y < row_end; ++y) {
 		for (int x = 0; x != gbuffer->width; ++x) {
-			size_t i = (size_t) y * gbuffer->width + x;
-			R rgb[3] = {RC(0.0), RC(0.0), RC(0.0)};
-			oracle_reservoir_t* res = out_reservoirs ? out_reservoirs + i : NULL;
-			if (gbuffer->primitive && gbuffer->primitive[i] == 0xffffffffu) {
-				if (res) {
-					res->light_index = -1;
-					res->w_sum = 0.0;
-					res->sample_value = 0.0;
-				}
-			} else {
-				shading_data_t sd;
-				sd.position = V3((R) g[0 * np + i], (R) g[1 * np + i], (R) g[2 * np + i]);
-				sd.normal = V3((R) g[3 * np + i], (R) g[4 * np + i], (R) g[5 * np + i]);
-				sd.outgoing = V3((R) g[6 * np + i], (R) g[7 * np + i], (R) g[8 * np + i]);
-				sd.lambert_outgoing = (R) g[9 * np + i];
-				sd.diffuse_albedo = V3((R) g[10 * np + i], (R) g[11 * np + i], (R) g[12 * np + i]);
-				sd.fresnel_0 = V3((R) g[13 * np + i], (R) g[14 * np + i], (R) g[15 * np + i]);
-				sd.roughness = (R) g[16 * np + i];
-				uint32_t seed = get_noise_accessor((uint32_t) x, (uint32_t) y, (uint32_t) gbuffer->width, random_number_x);
-				proposal_candidate_t candidates[OR_MAX_CANDIDATES];
-				const int proposal = settings->proposal && settings->light_sampling == ORACLE_LIGHT_RESERVOIR &&
-				                     scene->cluster_count > 0 && settings->candidate_count <= OR_MAX_CANDIDATES;
-				if (proposal) {
-					const float xp[3] = {g[0 * np + i], g[1 * np + i], g[2 * np + i]};
-					const float nn[3] = {g[3 * np + i], g[4 * np + i], g[5 * np + i]};
-					proposal_draw(scene, settings, xp, nn, (uint32_t) x, (uint32_t) y, (uint32_t) gbuffer->width,
-					              candidates);
-				}
-				shade_pixel(&c, &sd, seed, rgb, res, proposal ? candidates : NULL);
-			}
-			out_rgb[3 * i + 0] = (ORACLE_OUT_T) rgb[0];
-			out_rgb[3 * i + 1] = (ORACLE_OUT_T) rgb[1];
-			out_rgb[3 * i + 2] = (ORACLE_OUT_T) rgb[2];
+			const size_t i = (size_t) y * gbuffer->width + x;
+			render_pixel(&c, gbuffer, random_number_x, i, out_rgb + 3 * i, out_reservoirs ? out_reservoirs + i : NULL);
 		}
+	}
+	return 0;
+}
+
+/* Renders the listed pixels of one frame (indices y * width + x into the
+   full G-buffer), each with the noise seed of its own position, so that a
+   sample of a large frame reproduces that frame's pixels exactly.  Output k
+   (out_rgb[3k..3k+2], out_reservoirs[k]) belongs to pixels[k]. */
+int OR_EXPORT(oracle_render_pixels)(const oracle_scene_t* scene, const oracle_settings_t* settings,
+                                    const oracle_gbuffer_t* gbuffer, uint32_t random_number_x,
+                                    const uint32_t* pixels, size_t begin, size_t end, ORACLE_OUT_T* out_rgb,
+                                    oracle_reservoir_t* out_reservoirs) {
+	ctx_t c;
+	if (make_ctx(&c, scene, settings)) return 1;
+	const size_t np = (size_t) gbuffer->width * gbuffer->height;
+	for (size_t k = begin; k < end; ++k) {
+		if (pixels[k] >= np) return 1;
+		render_pixel(&c, gbuffer, random_number_x, pixels[k], out_rgb + 3 * k, out_reservoirs ? out_reservoirs + k : NULL);
 	}
 	return 0;
 }
