@@ -402,6 +402,31 @@ EXTERN_C int risltc_model_get_gradient(risltc_model_t* model, float* gradient, i
 /* One Adam step on the accumulated gradient, which it resets
    (stream-ordered on the context's stream). */
 EXTERN_C int risltc_model_apply_update(risltc_model_t* model);
+/* One RIS candidate of a pixel for risltc_model_train: the light drawn (an
+   index into the scene's lights) and its RIS weight p_hat / p. */
+typedef struct risltc_candidate_s {
+	int32_t light;
+	float weight;
+} risltc_candidate_t;
+/* One training step of the scene's model on caller-supplied candidates: the
+ * step risltc_shade takes after a frame when training is on, with the frame's
+ * candidates replaced by the caller's (no counterpart in the reference; for
+ * callers that make their own RIS candidates, and for tests of the gradient).
+ * Training pixels are i = phase + j * stride (phase < stride) of the G-buffer;
+ * candidates (device, width * height * candidate_count records, pixel-major)
+ * is read at training pixels only, candidates naming no light of the scene or
+ * with a weight of 0 are skipped.  The target is each cluster's share of the
+ * pixel's candidate weight (the scene's clusters, whose count must equal the
+ * model's); with shaded (device, one float per pixel: the shaded estimate's
+ * luminance) and reservoirs (device, the chosen light per pixel) the shadowed
+ * part of risltc_model_set_target_mix is added.  The gradient of the mean
+ * cross entropy over the training pixels is added to the model's gradient;
+ * an Adam step follows unless RISLTC_TRAIN_ACCUMULATE_ONLY is set.  Runs on
+ * the tensor cores or the CUDA cores as risltc_model_set_training_flags says.
+ * Stream-ordered on the context's stream. */
+EXTERN_C int risltc_model_train(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                                const risltc_candidate_t* candidates, uint32_t candidate_count, uint32_t stride,
+                                uint32_t phase, const float* shaded, const risltc_reservoir_t* reservoirs);
 /* Inputs: position (p - center) / half_extent. */
 EXTERN_C int risltc_model_set_input_transform(risltc_model_t* model, const float center[3], float half_extent);
 /* The model the scene's learned proposal uses (its cluster count must match

@@ -134,6 +134,9 @@ SIGNATURES = {
     "risltc_model_set_training_flags": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
     "risltc_model_get_gradient": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int]),
     "risltc_model_apply_update": (ctypes.c_int, [ctypes.c_void_p]),
+    "risltc_model_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer), ctypes.c_void_p,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
     "risltc_scene_set_model": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "risltc_model_logits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GBuffer), ctypes.c_void_p]),
     "risltc_gbuffer_heightfield": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Heightfield), ctypes.c_uint32,

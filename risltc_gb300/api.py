@@ -245,6 +245,19 @@ class Model:
               "risltc_model_get_gradient")
         return out
 
+    def train(self, scene, gbuffer, width, height, candidates, stride, phase=0, shaded=None, reservoirs=None,
+              primitive=None):
+        """risltc_model_train: one training step on caller-supplied candidates.
+        candidates: device tensor of width * height * M (light, weight) pairs
+        (int32 [P, M, 2] with the weights' bits in the second column, or
+        float32 viewed alike); shaded: float32 [P] and reservoirs: int32
+        [P, 4] (device) for the shadowed part, or None."""
+        m = candidates.shape[1]
+        g = _native.GBuffer(width, height, gbuffer.data_ptr(), None if primitive is None else primitive.data_ptr())
+        ptr = (lambda t: None if t is None else ctypes.c_void_p(t.data_ptr()))
+        check(self._lib.risltc_model_train(self.ctx.handle, scene.handle, ctypes.byref(g), ptr(candidates), m, stride,
+                                           phase, ptr(shaded), ptr(reservoirs)), "risltc_model_train")
+
     def apply_update(self):
         check(self._lib.risltc_model_apply_update(self._h), "risltc_model_apply_update")
 

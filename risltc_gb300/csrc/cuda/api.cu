@@ -626,6 +626,7 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 	t.inv_half_extent = m->inv_half_extent;
 	t.offsets = scene->clusters.offsets;
 	t.light_cluster = scene->clusters.light_cluster;
+	t.light_count = (uint32_t) scene->view.light_count;
 	t.primitive = gbuffer->primitive;
 	t.candidates = candidates;
 	t.candidate_count = candidate_count;
@@ -1419,6 +1420,27 @@ EXTERN_C int risltc_model_apply_update(risltc_model_t* model) {
 	if (!model) return RISLTC_ERROR_INVALID_ARGUMENT;
 	cudaSetDevice(model->ctx->device);
 	return cuda_status(launch_adam(model, model->ctx->stream));
+}
+
+static_assert(sizeof(risltc_candidate_t) == sizeof(risltc::ProposalCandidate) &&
+                  offsetof(risltc_candidate_t, weight) == offsetof(risltc::ProposalCandidate, pdf),
+              "candidate layout");
+static_assert(sizeof(risltc_reservoir_t) == sizeof(risltc::ReservoirRecord), "reservoir layout");
+
+EXTERN_C int risltc_model_train(risltc_ctx_t* ctx, const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
+                                const risltc_candidate_t* candidates, uint32_t candidate_count, uint32_t stride,
+                                uint32_t phase, const float* shaded, const risltc_reservoir_t* reservoirs) {
+	if (!ctx || !scene || scene->ctx != ctx || !scene->model || !gbuffer || !gbuffer->planes || !candidates ||
+	    gbuffer->width == 0 || gbuffer->height == 0 || candidate_count == 0 || candidate_count > 4096 ||
+	    stride == 0 || phase >= stride || (shaded && !reservoirs))
+		return RISLTC_ERROR_INVALID_ARGUMENT;
+	if (scene->clusters.count != scene->model->cluster_count) return RISLTC_ERROR_INVALID_ARGUMENT;
+	if ((uint64_t) gbuffer->width * gbuffer->height >= (1ull << 31)) return RISLTC_ERROR_TOO_LARGE;
+	cudaSetDevice(ctx->device);
+	return cuda_status(launch_training(ctx, ctx->stream, scene, gbuffer,
+	                                   reinterpret_cast<const risltc::ProposalCandidate*>(candidates),
+	                                   (int) candidate_count, stride, phase, shaded,
+	                                   reinterpret_cast<const risltc::ReservoirRecord*>(reservoirs)));
 }
 
 // ------------------------------------------------------------- G-buffers --

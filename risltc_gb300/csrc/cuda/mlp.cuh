@@ -168,6 +168,7 @@ struct MlpTrainParams {
 	float center[3], inv_half_extent;
 	const uint32_t* offsets;      // cluster offsets (light -> cluster via light_cluster)
 	const uint32_t* light_cluster;
+	uint32_t light_count;         // candidates naming another light are skipped
 	const uint32_t* primitive;
 	// Frame 0's candidates [pixel][candidate] after the candidate kernel wrote
 	// each training pixel's RIS weights w = p_hat / p into their pdf field.
@@ -280,9 +281,11 @@ static __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(MlpTrai
 			if (learn) {
 				for (int c = lane; c < pr.candidate_count; c += 32) {
 					const ProposalCandidate q = pr.candidates[(size_t) i * pr.candidate_count + c];
-					if (q.pdf > 0.0f) atomicAdd(&z[pr.light_cluster[q.light]], -wu * q.pdf / total * pr.inv_batch);
+					if (q.pdf > 0.0f && (uint32_t) q.light < pr.light_count)
+						atomicAdd(&z[pr.light_cluster[q.light]], -wu * q.pdf / total * pr.inv_batch);
 				}
-				if (lane == 0 && chosen >= 0 && ss > 0.0f) atomicAdd(&z[pr.light_cluster[chosen]], -ss * pr.inv_batch);
+				if (lane == 0 && chosen >= 0 && (uint32_t) chosen < pr.light_count && ss > 0.0f)
+					atomicAdd(&z[pr.light_cluster[chosen]], -ss * pr.inv_batch);
 			}
 			__syncwarp();
 		}

@@ -315,13 +315,13 @@ static __global__ void __launch_bounds__(kTcThreads, 1) mlp_train_tc_kernel(MlpT
 #pragma unroll 8
 			for (int c = 0; c < mc; ++c) {
 				const ProposalCandidate q = cand[c];
-				if (q.pdf > 0.0f) {
+				if (q.pdf > 0.0f && (uint32_t) q.light < pr.light_count) {
 					__nv_bfloat16* z = reinterpret_cast<__nv_bfloat16*>(
 					    tt_smem + kTtDz + tc_offset((int) tid, (int) pr.light_cluster[q.light], k_pad));
 					*z = __float2bfloat16_rn(__bfloat162float(*z) - unshadowed * q.pdf);
 				}
 			}
-			if (chosen >= 0 && ss > 0.0f) {
+			if (chosen >= 0 && (uint32_t) chosen < pr.light_count && ss > 0.0f) {
 				__nv_bfloat16* z = reinterpret_cast<__nv_bfloat16*>(
 				    tt_smem + kTtDz + tc_offset((int) tid, (int) pr.light_cluster[chosen], k_pad));
 				*z = __float2bfloat16_rn(__bfloat162float(*z) - ss * pr.inv_batch);
