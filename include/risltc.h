@@ -591,12 +591,19 @@ EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene,
  * most 64 calls are timed), split into RISLTC_PROFILE_PHASES phases:
  * phase_ms[0] the RIS candidate kernel (or the fused kernel), phase_ms[1] the
  * shading kernel (with its shadow rays, or up to queueing them), phase_ms[2]
- * the shadow-ray kernel and phase_ms[3] the resolve kernel (0 where a phase
- * is not a kernel of its own), and their number in calls; then enables
- * (enable != 0) or disables timing of the following calls.  phase_ms and
- * calls may be NULL.  Querying synchronises the stream. */
-#define RISLTC_PROFILE_PHASES 4
+ * the grouping of the shadow rays by light (bucket scan and scatter),
+ * phase_ms[3] the shadow-ray traversal kernel and phase_ms[4] the resolve
+ * kernel (0 where a phase is not a kernel of its own), and their number in
+ * calls; then enables (enable != 0) or disables timing of the following
+ * calls.  phase_ms and calls may be NULL.  Querying synchronises the
+ * stream. */
+#define RISLTC_PROFILE_PHASES 5
 EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, uint32_t* calls);
+
+/* The number of this library's own kernels launched through the context
+ * since it was created (shading, proposal, training and query kernels;
+ * memory copies and sets excluded). */
+EXTERN_C int risltc_ctx_launch_count(const risltc_ctx_t* ctx, uint64_t* launches);
 
 /* Synchronises the context's stream and returns the first error recorded by
    a kernel since the last check (RISLTC_OK if none). */

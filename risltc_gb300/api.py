@@ -107,13 +107,20 @@ class Context:
     def profile(self, enable=True):
         """Per-kernel CUDA-event times (ms) of the shading calls since the last
         call, then switches timing on or off.  Returns a dict: candidates
-        (or the fused kernel), shade, shadow_trace and resolve (0 where the
-        phase is not a kernel of its own), and calls."""
-        ms = (ctypes.c_float * 4)()
+        (or the fused kernel), shade, ray_sort (bucket scan and scatter),
+        shadow_trace and resolve (0 where the phase is not a kernel of its
+        own), and calls."""
+        ms = (ctypes.c_float * 5)()
         calls = ctypes.c_uint32(0)
         check(self._lib.risltc_ctx_profile(self._h, int(enable), ms, ctypes.byref(calls)), "risltc_ctx_profile")
-        return dict(candidates=float(ms[0]), shade=float(ms[1]), shadow_trace=float(ms[2]), resolve=float(ms[3]),
-                    calls=int(calls.value))
+        return dict(candidates=float(ms[0]), shade=float(ms[1]), ray_sort=float(ms[2]), shadow_trace=float(ms[3]),
+                    resolve=float(ms[4]), calls=int(calls.value))
+
+    def launch_count(self):
+        """risltc_ctx_launch_count: this library's kernels launched so far."""
+        n = ctypes.c_uint64(0)
+        check(self._lib.risltc_ctx_launch_count(self._h, ctypes.byref(n)), "risltc_ctx_launch_count")
+        return int(n.value)
 
     def close(self):
         if self._h:

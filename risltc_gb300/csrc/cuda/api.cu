@@ -78,7 +78,9 @@ struct risltc_ctx_s {
 	uint32_t inject;
 	int profiling;
 	int timed_calls;
-	cudaEvent_t events[64][5];
+	cudaEvent_t events[64][RISLTC_PROFILE_PHASES + 1];
+	// Kernels of this library launched through the context (risltc_ctx_launch_count).
+	uint64_t kernel_launches;
 	int events_created;
 };
 
@@ -302,7 +304,7 @@ EXTERN_C void risltc_ctx_destroy(risltc_ctx_t* ctx) {
 	}
 	if (ctx->batch_streams_created) cudaEventDestroy(ctx->batch_fork);
 	for (int i = 0; i < ctx->events_created; ++i)
-		for (int k = 0; k != 5; ++k) cudaEventDestroy(ctx->events[i][k]);
+		for (int k = 0; k != RISLTC_PROFILE_PHASES + 1; ++k) cudaEventDestroy(ctx->events[i][k]);
 	free(ctx);
 }
 
@@ -665,8 +667,11 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 		                           stream>>>(t);
 	}
 	cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess) ctx->kernel_launches += 1;
 	if (e != cudaSuccess || (m->training_flags & RISLTC_TRAIN_ACCUMULATE_ONLY)) return e;
-	return launch_adam(m, stream);
+	e = launch_adam(m, stream);
+	if (e == cudaSuccess) ctx->kernel_launches += 1;
+	return e;
 }
 
 // The model's logits for every pixel of the G-buffer into logits.
@@ -700,7 +705,9 @@ cudaError_t launch_logits(risltc_ctx_t* ctx, cudaStream_t stream, const risltc_m
 	const size_t tiles = ((size_t) gbuffer->width * gbuffer->height + risltc::kTcRows - 1) / risltc::kTcRows;
 	const int grid = (int) std::min<size_t>(tiles, (size_t) ctx->sm_count * 2);
 	risltc::mlp_logits_tc_kernel<<<grid, risltc::kTcThreads, risltc::mlp_tc_smem_bytes(m->cluster_count), stream>>>(q);
-	return cudaGetLastError();
+	const cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess) ctx->kernel_launches += 1;
+	return e;
 }
 
 int reserve_candidates(risltc_ctx_t* ctx, size_t need) {
@@ -801,6 +808,7 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		const int warps = (int) ((pixels + risltc::kProposalWarps - 1) / risltc::kProposalWarps);
 		e = risltc::launch_proposal(q, stream, std::min(warps, ctx->sm_count * 16));
 		if (e != cudaSuccess) return cuda_status(e);
+		ctx->kernel_launches += 1;
 	}
 	if (uses_ris_pipeline(settings)) {
 		// The reference's default configuration: candidate and shading
@@ -856,11 +864,15 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 		r.error = ctx->d_error;
 		e = risltc::launch_ris(r, stream, grid_for(ctx, pixels), grid_for(ctx, 2 * pixels * frame_count), events,
 		                       fast, (int) settings->tile, ctx->sm_count * 16);
+		// Candidates, then the estimator: sample, bucket scan, scatter, trace
+		// and resolve kernels, or one shading kernel with inline rays.
+		if (e == cudaSuccess) ctx->kernel_launches += r.samples ? 6 : 2;
 		if (e == cudaSuccess && train)
 			e = launch_training(ctx, stream, scene, gbuffer, sc.candidates, r.candidate_count, r.train_stride,
 			                    r.train_phase, r.train_shaded, r.records);
 	} else {
 		e = risltc::launch_shade(p, stream, grid_for(ctx, pixels), events, fast);
+		if (e == cudaSuccess) ctx->kernel_launches += 1;
 	}
 	return e == cudaSuccess ? RISLTC_OK : cuda_status(e);
 }
@@ -916,7 +928,7 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 	if (ctx->profiling && ctx->timed_calls < 64) {
 		int i = ctx->timed_calls++;
 		if (i >= ctx->events_created) {
-			for (int k = 0; k != 5; ++k) cudaEventCreate(&ctx->events[i][k]);
+			for (int k = 0; k != RISLTC_PROFILE_PHASES + 1; ++k) cudaEventCreate(&ctx->events[i][k]);
 			ctx->events_created = i + 1;
 		}
 		events = ctx->events[i];
@@ -930,12 +942,13 @@ EXTERN_C int risltc_shade(risltc_ctx_t* ctx, const risltc_scene_t* scene, const 
 
 namespace {
 
-// Five timing events for the autotuner, destroyed with the object.
+// Timing events of one shading call for the autotuner, destroyed with the
+// object.
 struct TuneEvents {
-	cudaEvent_t e[5] = {};
+	cudaEvent_t e[RISLTC_PROFILE_PHASES + 1] = {};
 	int created = 0;
 	cudaError_t create() {
-		for (; created != 5; ++created) {
+		for (; created != RISLTC_PROFILE_PHASES + 1; ++created) {
 			cudaError_t r = cudaEventCreate(&e[created]);
 			if (r != cudaSuccess) return r;
 		}
@@ -1184,7 +1197,14 @@ EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene,
 	cudaSetDevice(ctx->device);
 	cudaError_t e = risltc::launch_trace_exact(scene->view, (const float4*) rays, ray_count, hits, ctx->d_error,
 	                                           ctx->stream, grid_for(ctx, ray_count));
+	if (e == cudaSuccess) ctx->kernel_launches += 1;
 	return cuda_status(e);
+}
+
+EXTERN_C int risltc_ctx_launch_count(const risltc_ctx_t* ctx, uint64_t* launches) {
+	if (!ctx || !launches) return RISLTC_ERROR_INVALID_ARGUMENT;
+	*launches = ctx->kernel_launches;
+	return RISLTC_OK;
 }
 
 EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, uint32_t* calls) {
@@ -1419,7 +1439,9 @@ EXTERN_C int risltc_model_get_gradient(risltc_model_t* model, float* gradient, i
 EXTERN_C int risltc_model_apply_update(risltc_model_t* model) {
 	if (!model) return RISLTC_ERROR_INVALID_ARGUMENT;
 	cudaSetDevice(model->ctx->device);
-	return cuda_status(launch_adam(model, model->ctx->stream));
+	const cudaError_t e = launch_adam(model, model->ctx->stream);
+	if (e == cudaSuccess) model->ctx->kernel_launches += 1;
+	return cuda_status(e);
 }
 
 static_assert(sizeof(risltc_candidate_t) == sizeof(risltc::ProposalCandidate) &&
@@ -1490,5 +1512,7 @@ EXTERN_C int risltc_gbuffer_heightfield(risltc_ctx_t* ctx, const risltc_heightfi
 	p.primitive = primitive;
 	cudaSetDevice(ctx->device);
 	risltc::heightfield_gbuffer_kernel<<<grid_for(ctx, (size_t) width * height), 128, 0, ctx->stream>>>(p);
-	return cuda_status(cudaGetLastError());
+	const cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess) ctx->kernel_launches += 1;
+	return cuda_status(e);
 }

@@ -352,15 +352,17 @@ inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid,
 		if (e != cudaSuccess) return e;
 		if (events) cudaEventRecord(events[2], stream);
 		e = launch_shadow_sort(p, stream, grid);
-		if (e == cudaSuccess) e = launch_shadow_trace(p, stream, trace_grid);
 		if (e != cudaSuccess) return e;
 		if (events) cudaEventRecord(events[3], stream);
-		e = launch_ris_resolve(p, stream, grid);
+		e = launch_shadow_trace(p, stream, trace_grid);
+		if (e != cudaSuccess) return e;
 		if (events) cudaEventRecord(events[4], stream);
+		e = launch_ris_resolve(p, stream, grid);
+		if (events) cudaEventRecord(events[5], stream);
 	} else {
 		e = launch_ris_shade(p, stream, grid);
 		if (events)
-			for (int k = 2; k != 5; ++k) cudaEventRecord(events[k], stream);
+			for (int k = 2; k != RISLTC_PROFILE_PHASES + 1; ++k) cudaEventRecord(events[k], stream);
 	}
 	return e;
 }

@@ -14,7 +14,7 @@ cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cu
 		shade_kernel<ExactNumerics, ExactNumerics><<<grid, 128, 0, stream>>>(p);
 	cudaError_t e = cudaGetLastError();
 	if (events)
-		for (int k = 1; k != 5; ++k) cudaEventRecord(events[k], stream);
+		for (int k = 1; k != RISLTC_PROFILE_PHASES + 1; ++k) cudaEventRecord(events[k], stream);
 	return e;
 }
 cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int grid_cap, int tile) {

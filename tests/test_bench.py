@@ -11,7 +11,7 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_prints_one_contract_line():
     cmd = [sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--width", "96", "--height", "54",
-           "--lights", "32", "--triangles", "500", "--steps", "3", "--warmup", "3", "--cpu-seconds", "0.2"]
+           "--lights", "32", "--clusters", "8", "--triangles", "500", "--steps", "3", "--warmup", "3", "--cpu-seconds", "0.2"]
     out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=REPO)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [line for line in out.stdout.splitlines() if line.strip()]
@@ -19,8 +19,22 @@ def test_reference_arm_prints_one_contract_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "Gsamples/s" and d["value"] > 0
     assert (d["steps"], d["warmup"], d["n_gpus"], d["higher_is_better"]) == (3, 3, 1, True)
-    assert d["metric"].startswith("Gsamples/s (shadowed single frame: 96x54 fBm heightfield, 32 polygon lights")
+    assert d["metric"].startswith("Gsamples/s (many-lights frame: 96x54 fBm heightfield, 32 polygon lights (3-8 "
+                                  "vertices) in 8 k-means clusters")
     assert d["vs_baseline"] is None
     cpu = d["cpu_baseline"]
     assert cpu["kind"] == "port" and cpu["cores"] >= 1 and cpu["value"] == d["value"] and cpu["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_default_workload_is_the_headline_configuration():
+    """With no flags the bench runs the configuration the headline metric is
+    quoted on: 1080p, 16,384 lights in 256 clusters, 1M occluders, M = 32."""
+    sys.path.insert(0, REPO)
+    import bench
+    a = bench.parse([])
+    assert (a.workload, a.width, a.height, a.lights, a.clusters, a.triangles, a.candidates, a.spp) == (
+        "headline", 1920, 1080, 16384, 256, 1_000_000, 32, 4)
+    assert bench.is_headline(a) and bench.metric_name(a) == bench.HEADLINE_METRIC
+    b = bench.parse(["--workload", "throughput"])
+    assert (b.lights, b.triangles, b.clusters) == (1024, 200_000, 0)

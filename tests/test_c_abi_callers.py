@@ -156,6 +156,8 @@ def test_device_routines_equal_oracle(gpu, tmp_path):
         r = np.ascontiguousarray(rnd[c])
         total = ol.oracle_f32_psa_sample(int(want_vc), poly.ctypes.data, samples, r.ctypes.data,
                                          want_dirs.ctypes.data, None)
-        assert psa[c] == np.float32(total), c
-        assert np.array_equal(dirs[c], want_dirs), c
+        assert psa[c] == np.float32(total) or (np.isnan(psa[c]) and np.isnan(total)), c
+        # A sliver left by the clipper can have no projected solid angle; its
+        # samples are NaN on both sides.
+        assert np.array_equal(dirs[c], want_dirs, equal_nan=True), c
     assert partial > 100  # the clipped cases were exercised
