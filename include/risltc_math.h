@@ -12,7 +12,9 @@
  * GPU produce identical bits.
  *
  * Methods (coefficients fitted for this project by least squares on
- * Chebyshev nodes, see risltc_gb300/csrc/fit_math_coeffs.py):
+ * Chebyshev nodes, weighted to relative error; the script
+ * risltc_gb300/csrc/fit_math_coeffs.py refits them by that method and
+ * measures the FP32 error of the committed values):
  *  - atan: reduction to [0,1] by atan(x) = pi/2 - atan(1/x), then an odd
  *    polynomial r*P(r^2) of degree 21.  Max error 1.5 ulp on [0,1].
  *  - sin/cos: Cody-Waite reduction by pi/2 (three-part constant, valid for

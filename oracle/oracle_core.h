@@ -1,4 +1,6 @@
 /* oracle_core.h - CPU restatement of risltc's per-pixel shading path.
+ * Restates upstream risltc routines (GPLv3; the polygon_sampling.glsl parts
+ * also BSD-3, whose notice is retained in NOTICE).
  *
  * TEST INFRASTRUCTURE.  This is the oracle: the checker the CUDA kernels are
  * compared against, and the CPU baseline that bench.py times.  The product

@@ -1,9 +1,10 @@
 """Build the pinning reference: the reference renderer's own shading-pass GLSL,
 lowered to C++ (glsl_lower.py) and compiled with g++ into oracle/_ref/.
 
-Test infrastructure.  Runs only where the reference sources are present
-(RISLTC_REFERENCE_DIR, default /root/reference); the GPU machine never needs it,
-because the reference's outputs are committed as fixtures under tests/golden/.
+Test infrastructure.  Runs only where the reference sources are present, in
+the directory named by the environment variable RISLTC_REFERENCE_DIR (no
+default); machines without them never need it, because the reference's
+outputs are committed as fixtures under tests/golden/.
 
 Each shader specialisation (the defines of main.c:962-990) is its own shared
 library, named by its configuration tag.
@@ -17,8 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 REPO = os.path.dirname(ORACLE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
-REFERENCE_DIR = os.environ.get("RISLTC_REFERENCE_DIR", "/root/reference")
-SHADER_DIR = os.path.join(REFERENCE_DIR, "src", "shaders")
+REFERENCE_DIR = os.environ.get("RISLTC_REFERENCE_DIR", "")
+SHADER_DIR = os.path.join(REFERENCE_DIR, "src", "shaders") if REFERENCE_DIR else ""
 
 sys.path.insert(0, HERE)
 import glsl_lower  # noqa: E402
@@ -28,7 +29,7 @@ TECHNIQUES = ["baseline", "area_turk", "projected_solid_angle", "projected_solid
 
 
 def reference_available():
-    return os.path.isfile(os.path.join(SHADER_DIR, "shading_pass.frag.glsl"))
+    return bool(SHADER_DIR) and os.path.isfile(os.path.join(SHADER_DIR, "shading_pass.frag.glsl"))
 
 
 def _defines(cfg):

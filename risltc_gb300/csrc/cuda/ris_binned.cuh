@@ -22,6 +22,7 @@
 // Every p_hat is computed by the same operations on the same values as in
 // ris_candidates_kernel and the reservoir sees them in the same order, so the
 // reservoir records are bit-identical.
+// Restates upstream risltc routines (GPLv3): see NOTICE.
 #pragma once
 #include <algorithm>
 #include <atomic>

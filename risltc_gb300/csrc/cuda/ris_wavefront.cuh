@@ -18,6 +18,7 @@
 // the same order, so the pixels are bit-identical to ris_shade_kernel's.
 // Used for one sample per technique (SAMPLE_COUNT == 1, the reference's
 // default) with shadows on.
+// Restates upstream risltc routines (GPLv3): see NOTICE.
 #pragma once
 #include "ris_kernels.cuh"
 

@@ -1,5 +1,6 @@
 // shade_kernel.cuh - the per-pixel shading kernel and the shadow-ray kernel.
 // Instantiated by shade_exact.cu and shade_fast.cu with one numerics policy.
+// Restates upstream risltc routines (GPLv3): see NOTICE.
 #pragma once
 #include "shade_psa.cuh"
 

@@ -1,6 +1,8 @@
 // shade_psa.cuh - projected solid angle sampling of convex polygons on the
 // device (polygon_sampling.glsl:231-828), plus the BRDF and MIS weights
 // (brdfs.glsl:43-93, shading_pass.frag.glsl:219-269).
+// Restates upstream risltc routines (GPLv3; the polygon_sampling.glsl parts
+// also BSD-3, whose notice is retained in NOTICE).
 #pragma once
 #include "shade_device.cuh"
 

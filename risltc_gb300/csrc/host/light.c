@@ -1,4 +1,5 @@
 /* Host model of polygonal lights and of the per-frame noise constants.
+ * Restates upstream risltc code (GPLv3): see NOTICE.
  *
  * Restates src/polygonal_light.c, write_lights (src/main.c:456-490),
  * set_noise_constants (src/noise_table.c:24-28) and wang_random_number

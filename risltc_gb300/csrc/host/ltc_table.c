@@ -1,4 +1,5 @@
 /* LTC tables without Vulkan: the quantisation of load_ltc_table
+ * Restates upstream risltc code (GPLv3): see NOTICE.
  * (src/ltc_table.c:82-116) and its sampling constants (:184-192), the fit
  * file reader (:31-50), and a seeded synthetic fit that stands in for the
  * reference's fit files (not distributed with the reference).

@@ -1,6 +1,7 @@
 """Generates the golden fixtures under tests/golden/ from the reference itself.
 
-Runs only where the reference sources are present (default /root/reference):
+Runs only where the reference sources are present, in the directory named by
+the environment variable RISLTC_REFERENCE_DIR (no default):
 the reference's shading pass (src/shaders/shading_pass.frag.glsl and its
 includes, lowered to C++ by oracle/ref/glsl_lower.py), its clip_polygon, and
 its plain-C light model (src/polygonal_light.c) are compiled and executed on

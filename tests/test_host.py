@@ -260,3 +260,15 @@ def test_bvh_shadow_answers_equal_brute_force(kind):
     unshadowed = oracle.OracleScene(hs.lights, hs.max_vertex_count, hs.ltc0, hs.ltc1, hs.ltc_constants)
     c, _, _ = oracle.render(unshadowed, st, hs.gbuffer, hs.width, hs.height, rn, reservoirs=False)
     assert not np.array_equal(a, c)  # the occluders do shadow the frame
+
+
+def test_transcendental_coefficients_meet_their_error_bounds():
+    """include/risltc_math.h's polynomial coefficients, evaluated in FP32 as
+    the header does, stay within the bounds it states (the fit script's own
+    check; it also refits them by the header's method)."""
+    import subprocess
+    import sys
+    script = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "risltc_gb300", "csrc",
+                          "fit_math_coeffs.py")
+    out = subprocess.run([sys.executable, script], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
