@@ -48,9 +48,14 @@ float oracle_f32_psa_sample(uint32_t vc, const float* xyz, uint32_t count, const
 	projected_solid_angle_polygon_t p;
 	g_oracle_fast_atan = 0;
 	g_oracle_biased_psa = 0;
-	prepare_projected_solid_angle_polygon_sampling(&p, vc, v, vc + 1);
+	/* The slot count the routines wrap at: vc + 1 (the first vertex
+	   repeated), at most the struct's OR_MAXP slots; a polygon that fills
+	   them all (an 8-gon clipped to 9 vertices) wraps to slot 0 itself, as
+	   in the shading path. */
+	const uint32_t maxp = vc + 1 < OR_MAXP ? vc + 1 : OR_MAXP;
+	prepare_projected_solid_angle_polygon_sampling(&p, vc, v, maxp);
 	for (uint32_t k = 0; k != count; ++k) {
-		vec3_t d = sample_projected_solid_angle_polygon(&p, V2(rnd[2 * k], rnd[2 * k + 1]), vc + 1);
+		vec3_t d = sample_projected_solid_angle_polygon(&p, V2(rnd[2 * k], rnd[2 * k + 1]), maxp);
 		out_dirs[3 * k] = d.x;
 		out_dirs[3 * k + 1] = d.y;
 		out_dirs[3 * k + 2] = d.z;

@@ -188,6 +188,147 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 	return true;
 }
 
+// ---------------------------------------------------------------------------
+// The same candidate with both spaces in the two lanes of Blackwell's paired
+// FP32 instructions (FADD2 / FMUL2 / FFMA2 on float2; lane .x the shading
+// space, lane .y the cosine space).  Both spaces walk the same vertices, so
+// every transform, dot product, scale and edge-integral step of the two
+// spaces is one paired instruction.  Each lane performs the scalar version's
+// operations on the same operands in the same order, and a paired IEEE add
+// or multiply rounds each lane exactly as the scalar one does: the values are
+// bit-identical.  Exact numerics keeps every multiply and add separate; fast
+// numerics contracts them into paired fused multiply-adds.
+#ifndef RISLTC_CANDIDATE_PAIRS
+#define RISLTC_CANDIDATE_PAIRS 1
+#endif
+
+RL_DEV float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+RL_DEV float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+RL_DEV float2 pair(float a) { return make_float2(a, a); }
+// a * b + c, contracted in fast numerics.
+template <class P> RL_DEV float2 mad2(float2 a, float2 b, float2 c) { return add2(mul2(a, b), c); }
+template <> RL_DEV float2 mad2<FastNumerics>(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+struct f3x2 {
+	float2 x, y, z;
+};
+// mat4x3 * vec4(p, 1) in both lanes: ((c0 p.x + c1 p.y) + c2 p.z) + c3.
+struct mat43x2 {
+	f3x2 c[4];
+};
+template <class P> RL_DEV f3x2 mul_point2(const mat43x2& m, float4 q) {
+	const float2 px = pair(q.x), py = pair(q.y), pz = pair(q.z);
+	f3x2 r;
+	r.x = add2(mad2<P>(m.c[2].x, pz, mad2<P>(m.c[1].x, py, mul2(m.c[0].x, px))), m.c[3].x);
+	r.y = add2(mad2<P>(m.c[2].y, pz, mad2<P>(m.c[1].y, py, mul2(m.c[0].y, px))), m.c[3].y);
+	r.z = add2(mad2<P>(m.c[2].z, pz, mad2<P>(m.c[1].z, py, mul2(m.c[0].z, px))), m.c[3].z);
+	return r;
+}
+template <class P> RL_DEV float2 dot2(const f3x2& a, const f3x2& b) {
+	return mad2<P>(a.z, b.z, mad2<P>(a.y, b.y, mul2(a.x, b.x)));
+}
+template <class P> RL_DEV f3x2 normalize2(const f3x2& a) {
+	const float2 d = dot2<P>(a, a);
+	const float2 s = make_float2(P::rsqrt(d.x), P::rsqrt(d.y));
+	return {mul2(a.x, s), mul2(a.y, s), mul2(a.z, s)};
+}
+// integrate_edge on both lanes.
+template <class P> RL_DEV float2 integrate_edge2(const f3x2& v1, const f3x2& v2) {
+	const float2 x = dot2<P>(v1, v2);
+	const float2 y = make_float2(fabsf(x.x), fabsf(x.y));
+	const float2 a = add2(pair(0.8543985f), mul2(mad2<P>(pair(0.0145206f), y, pair(0.4965155f)), y));
+	const float2 b = add2(pair(3.4175940f), mul2(add2(pair(4.1616724f), y), y));
+	float2 ts = make_float2(P::div(a.x, b.x), P::div(a.y, b.y));
+	if (!(x.x > 0.0f)) ts.x = 0.5f * P::rsqrt(fmax_glsl(1.0f - x.x * x.x, 1e-7f)) - ts.x;
+	if (!(x.y > 0.0f)) ts.y = 0.5f * P::rsqrt(fmax_glsl(1.0f - x.y * x.y, 1e-7f)) - ts.y;
+	const float2 cz = add2(mul2(v1.x, v2.y), mul2(make_float2(-v1.y.x, -v1.y.y), v2.x));
+	return mul2(cz, ts);
+}
+
+template <class P>
+RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+	const float4 head = __ldg(record), pl = __ldg(record + 1);
+	const uint32_t n = __float_as_uint(head.w);
+	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
+	const bool flip = plane_dot(mk3(f[0], f[1], f[2]), plane) < 0.0f;
+	// Lane .x: world to shading space (y negated on a flip); lane .y: world
+	// to cosine space (the y-flipped matrix on a flip).
+	const float* ms = f + 7;
+	const float* mc = f + (flip ? 31 : 19);
+	mat43x2 t;
+#pragma unroll
+	for (int c = 0; c != 4; ++c) {
+		t.c[c].x = make_float2(ms[3 * c], mc[3 * c]);
+		t.c[c].y = make_float2(ms[3 * c + 1], mc[3 * c + 1]);
+		t.c[c].z = make_float2(ms[3 * c + 2], mc[3 * c + 2]);
+	}
+	float4 q = __ldg(record + 2);
+	f3x2 v = mul_point2<P>(t, q);
+	if (flip) v.y.x = -v.y.x;
+	q = __ldg(record + 3);
+	uint32_t above_s = v.z.x > 0.0f ? 1u : 0u, above_c = v.z.y > 0.0f ? 1u : 0u;
+	const f3x2 first = normalize2<P>(v);
+	f3x2 prev = first;
+	float2 r = pair(0.0f);
+#pragma unroll 1
+	for (uint32_t j = 1; j != n; ++j) {
+		v = mul_point2<P>(t, q);
+		if (flip) v.y.x = -v.y.x;
+		q = __ldg(record + 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
+		above_s += v.z.x > 0.0f ? 1u : 0u;
+		above_c += v.z.y > 0.0f ? 1u : 0u;
+		const f3x2 cur = normalize2<P>(v);
+		r = add2(r, integrate_edge2<P>(prev, cur));
+		prev = cur;
+	}
+	r = add2(r, integrate_edge2<P>(prev, first));
+	const bool partial_s = above_s != n && above_s != 0, partial_c = above_c != n && above_c != 0;
+	if ((partial_s || partial_c) && !allow_clip) return false;
+	float integral[2];
+	bool away[2];
+	const uint32_t above[2] = {above_s, above_c};
+	const float sum[2] = {r.x, r.y};
+#pragma unroll
+	for (int s = 0; s != 2; ++s) {
+		float rs = sum[s];
+		bool a = false;
+		if (above[s] == n) {
+			rs = fabsf(rs);
+		} else if (above[s] == 0) {
+			rs = 0.0f;
+			a = true;
+		} else {
+			const float* m = s == 0 ? ms : mc;
+			mat43 ts;
+#pragma unroll
+			for (int c = 0; c != 4; ++c) ts.c[c] = mk3(m[3 * c], m[3 * c + 1], m[3 * c + 2]);
+			rs = clipped_integral<P>(ts, record, n, s == 0 && flip);
+			a = rs < 0.0f;
+			rs = a ? 0.0f : rs;
+		}
+		integral[s] = rs;
+		away[s] = a;
+	}
+	const f3 radiance = mk3(head.x, head.y, head.z);
+	f3 result = splat(0.0f);
+	const f3 diffuse = away[0] ? splat(0.0f) : mul(scale(mk3(f[3], f[4], f[5]), integral[0]), radiance);
+	result = add(result, diffuse);
+	const f3 ggx = away[1] ? splat(0.0f) : mul(splat(integral[1] * f[6]), radiance);
+	const f3 color = add(result, ggx);
+	p_hat = P::sqrt(dot(color, color));
+	return true;
+}
+
+// The candidate evaluation the binned kernel uses.
+template <class P>
+RL_DEV bool evaluate_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+#if RISLTC_CANDIDATE_PAIRS
+	return binned_candidate_pair<P>(f, record, allow_clip, p_hat);
+#else
+	return binned_candidate<P>(f, record, allow_clip, p_hat);
+#endif
+}
+
 template <class P, int kPixels, int kChunk>
 __global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
 ris_candidates_binned_kernel(RisParams pr) {
@@ -307,7 +448,7 @@ ris_candidates_binned_kernel(RisParams pr) {
 							const uint32_t slot = item & 1023u;
 							const int32_t l = (int32_t) (item >> 10);
 							float ph;
-							if (binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph)) {
+							if (evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph)) {
 								phat[slot] = ph;
 							} else {
 								const uint32_t d = atomicAdd(&tile.deferred_count, 1u);
@@ -320,8 +461,8 @@ ris_candidates_binned_kernel(RisParams pr) {
 						const uint32_t d = pending - 32 + lane;
 						const uint32_t slot = tile.deferred[d] & 1023u;
 						float ph = 0.0f;
-						binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[d] >> 10)),
-						                    true, ph);
+						evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[d] >> 10)),
+						                      true, ph);
 						phat[slot] = ph;
 						__syncwarp();
 						if (lane == 0) tile.deferred_count = pending - 32;
@@ -333,8 +474,8 @@ ris_candidates_binned_kernel(RisParams pr) {
 				if (lane < rest) {
 					const uint32_t slot = tile.deferred[lane] & 1023u;
 					float ph = 0.0f;
-					binned_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[lane] >> 10)),
-					                    true, ph);
+					evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[lane] >> 10)),
+					                      true, ph);
 					phat[slot] = ph;
 				}
 				__syncwarp();

@@ -110,9 +110,10 @@ def test_shadowed_1080p_1024_lights_200k_occluders(rl, shadowed_1080p):
     hs = shadowed_1080p
     frames = compare_frames(rl, hs, rlm.settings(candidates=32), lambda f: oracle.make_settings(candidates=32), 4,
                             sample_pixels(hs, SAMPLE_PIXELS, 11))
-    # The sample is lit and shadowed: some pixels see light, some of the
-    # chosen lights are occluded.
-    assert (frames[0].sum(1) > 0).mean() > 0.5
+    # The sample holds both lit pixels and pixels whose light is occluded or
+    # faces away.
+    lit = (frames[0].sum(1) > 0).mean()
+    assert 0.1 < lit < 0.99
 
 
 def test_shadowed_1080p_fast_numerics_within_tolerance(rl, shadowed_1080p):

@@ -117,8 +117,11 @@ def test_training_gradient_matches_oracle(setup, k, m, stride, phase, shadowed):
     chosen = rng.integers(-1, n_lights, p).astype(np.int32)
     res = np.zeros((p, 4), np.int32)
     res[:, 0] = chosen
+    # Some background pixels, which the step must skip.
+    primitive = hs.primitive.copy()
+    primitive[::11] = 0xFFFFFFFF
     g = torch.from_numpy(hs.gbuffer).cuda()
-    prim = torch.from_numpy(hs.primitive.view(np.int32)).cuda()
+    prim = torch.from_numpy(primitive.view(np.int32)).cuda()
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
     d_cand, d_shaded, d_res = dev(cand), dev(shaded), dev(res)
     grads = {}
@@ -133,7 +136,7 @@ def test_training_gradient_matches_oracle(setup, k, m, stride, phase, shadowed):
     model.close()
     train = np.arange(phase, p, stride)
     inv_batch = np.float32(1.0) / np.float32(train.size)
-    valid = hs.primitive[train] != 0xFFFFFFFF
+    valid = primitive[train] != 0xFFFFFFFF
     assert (~valid).any() and valid.any()
     feats = mlp_numpy.encode(hs.gbuffer[:, train], center, half)
     args = (params, k, feats, lights[train], weights[train], light_cluster, n_lights, inv_batch, valid)
