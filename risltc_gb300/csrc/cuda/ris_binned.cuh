@@ -201,6 +201,11 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 #ifndef RISLTC_CANDIDATE_PAIRS
 #define RISLTC_CANDIDATE_PAIRS 1
 #endif
+// Unroll factor of the paired vertex loop.
+#ifndef RISLTC_PAIR_UNROLL
+#define RISLTC_PAIR_UNROLL 1
+#endif
+constexpr int kPairUnroll = RISLTC_PAIR_UNROLL;
 
 RL_DEV float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 RL_DEV float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -270,7 +275,7 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 	const f3x2 first = normalize2<P>(v);
 	f3x2 prev = first;
 	float2 r = pair(0.0f);
-#pragma unroll 1
+#pragma unroll kPairUnroll
 	for (uint32_t j = 1; j != n; ++j) {
 		v = mul_point2<P>(t, q);
 		if (flip) v.y.x = -v.y.x;
