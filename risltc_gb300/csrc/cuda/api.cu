@@ -11,8 +11,7 @@
 #include "mlp.cuh"
 #include "mlp_tc.cuh"
 #include "mlp_train_tc.cuh"
-#include "ris_binned.cuh"
-#include "ris_wavefront.cuh"
+#include "ris_batch.cuh"
 
 // Triangles per BVH leaf before the SAH is consulted.
 #ifndef RISLTC_BVH_LEAF
@@ -753,6 +752,47 @@ int reserve_records(risltc_ctx_t* ctx, size_t need) {
 	return RISLTC_OK;
 }
 
+// The parameters of the candidate/estimator kernels of one frame set of the
+// default configuration (LTC-CP, reservoir, one light sample) with its
+// share of the scratch: the reservoir records, p_hat slots and, with the ray
+// queue, the wavefront buffers.
+risltc::RisParams ris_params(const risltc_ctx_t* ctx, const Scratch& sc, const risltc_scene_t* scene,
+                             const risltc_gbuffer_t* gbuffer, const risltc_settings_t* settings, uint32_t noise_seed,
+                             uint32_t animate, uint32_t frame_count, float* out_rgb, double* accum,
+                             risltc_reservoir_t* reservoirs, bool ray_queue) {
+	risltc::RisParams r;
+	memset(&r, 0, sizeof(r));
+	r.scene = scene->view;
+	r.gbuffer = gbuffer->planes;
+	r.primitive = gbuffer->primitive;
+	r.width = gbuffer->width;
+	r.height = gbuffer->height;
+	r.candidate_count = (int) settings->candidate_count;
+	r.mis_heuristic = (int) settings->mis_heuristic;
+	r.sample_count = (int) settings->sample_count;
+	r.mis_visibility_estimate = settings->mis_visibility_estimate;
+	r.fast_atan = (int) settings->fast_atan;
+	r.shadows = (int) settings->shadows;
+	r.noise_seed = noise_seed;
+	r.animate = animate;
+	r.frame_count = frame_count;
+	r.records = sc.records;
+	r.p_hat_scratch = sc.p_hat;
+	if (ray_queue) {
+		r.samples = sc.samples;
+		r.staged = sc.staged;
+		r.rays = sc.rays;
+		r.light_rays = sc.light_rays;
+		r.ray_count = sc.ray_count;
+		r.hits = sc.hits;
+	}
+	r.out_rgb = out_rgb;
+	r.accum = accum;
+	r.reservoirs = reservoirs;
+	r.error = ctx->d_error;
+	return r;
+}
+
 // Enqueues one frame set on `stream` with its scratch already reserved.
 int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const risltc_scene_t* scene,
               const risltc_gbuffer_t* gbuffer, const risltc_settings_t* settings, uint32_t noise_seed,
@@ -813,24 +853,8 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 	if (uses_ris_pipeline(settings)) {
 		// The reference's default configuration: candidate and shading
 		// kernels with reservoir records in between.
-		risltc::RisParams r;
-		memset(&r, 0, sizeof(r));
-		r.scene = p.scene;
-		r.gbuffer = p.gbuffer;
-		r.primitive = p.primitive;
-		r.width = p.width;
-		r.height = p.height;
-		r.candidate_count = p.candidate_count;
-		r.mis_heuristic = p.mis_heuristic;
-		r.sample_count = p.sample_count;
-		r.mis_visibility_estimate = p.mis_visibility_estimate;
-		r.fast_atan = p.fast_atan;
-		r.shadows = p.shadows;
-		r.noise_seed = p.noise_seed;
-		r.animate = p.animate;
-		r.frame_count = p.frame_count;
-		r.records = sc.records;
-		r.p_hat_scratch = sc.p_hat;
+		risltc::RisParams r = ris_params(ctx, sc, scene, gbuffer, settings, noise_seed, animate, frame_count, out_rgb,
+		                                 accum, reservoirs, uses_ray_queue(scene, settings, pixels * frame_count));
 		r.candidates = uses_proposal(settings) ? sc.candidates : nullptr;
 		const risltc_model_t* model = scene->model;
 		const bool train = settings->proposal == risltc_proposal_learned && model && model->training;
@@ -850,18 +874,6 @@ int shade_one(risltc_ctx_t* ctx, cudaStream_t stream, const Scratch& sc, const r
 				r.train_shaded = mm->d_shaded;
 			}
 		}
-		if (uses_ray_queue(scene, settings, pixels * frame_count)) {
-			r.samples = sc.samples;
-			r.staged = sc.staged;
-			r.rays = sc.rays;
-			r.light_rays = sc.light_rays;
-			r.ray_count = sc.ray_count;
-			r.hits = sc.hits;
-		}
-		r.out_rgb = out_rgb;
-		r.accum = accum;
-		r.reservoirs = reservoirs;
-		r.error = ctx->d_error;
 		e = risltc::launch_ris(r, stream, grid_for(ctx, pixels), grid_for(ctx, 2 * pixels * frame_count), events,
 		                       fast, (int) settings->tile, ctx->sm_count * 16);
 		// Candidates, then the estimator: sample, bucket scan, scatter, trace
@@ -1056,6 +1068,102 @@ EXTERN_C int risltc_autotune_batch(risltc_ctx_t* ctx, risltc_batch_item_t* items
 	return RISLTC_OK;
 }
 
+namespace {
+
+uint32_t tile_pixels(risltc_tile_t tile) {
+	switch (tile) {
+	case risltc_tile_16x8:
+	case risltc_tile_16x4:
+		return 16;
+	case risltc_tile_8x8:
+		return 8;
+	default:
+		return 32;
+	}
+}
+
+// Whether every item runs the default configuration with plain RIS
+// candidates and its shadow rays through the ray queue, all with the same
+// numerics and binned tile shape, and each group of kBatchItems items holds
+// fewer than 2^31 pixel-frames: then risltc_shade_batch runs one launch per
+// phase for the whole batch.
+bool batch_is_fused(const risltc_batch_item_t* items, uint32_t item_count) {
+	size_t group = 0;
+	for (uint32_t i = 0; i != item_count; ++i) {
+		const risltc_batch_item_t& it = items[i];
+		const size_t pf = (size_t) it.gbuffer.width * it.gbuffer.height * it.frame_count;
+		if (!uses_ray_queue(it.scene, &it.settings, pf) || uses_proposal(&it.settings) ||
+		    it.settings.numerics != items[0].settings.numerics || it.settings.tile != items[0].settings.tile ||
+		    it.settings.tile == risltc_tile_per_pixel)
+			return false;
+		group = (i % risltc::kBatchItems == 0) ? pf : group + pf;
+		if (group >= (1ull << 31)) return false;
+	}
+	return item_count > 0;
+}
+
+// The whole batch with one launch per phase (groups of kBatchItems items),
+// on the context's stream; the scratch is reserved.  queues: the items' ray
+// queues, followed by the trace's fetch cursor.
+int shade_batch_fused(risltc_ctx_t* ctx, const risltc_batch_item_t* items, uint32_t item_count, size_t queues) {
+	const risltc_tile_t tile = items[0].settings.tile;
+	const bool fast = items[0].settings.numerics == risltc_numerics_fast;
+	const uint32_t px_per_tile = tile_pixels(tile);
+	size_t r_off = 0, w_off = 0, l_off = 0;
+	for (uint32_t g0 = 0; g0 < item_count; g0 += risltc::kBatchItems) {
+		const uint32_t gn = std::min<uint32_t>(item_count - g0, (uint32_t) risltc::kBatchItems);
+		risltc::RisBatch b;
+		memset(&b, 0, sizeof(b));
+		b.count = gn;
+		b.p_hat_scratch = ctx->d_phat;
+		b.ray_cursor = ctx->d_ray_count + 2 * queues;
+		uint32_t tiles = 0, pixels = 0, pfs = 0;
+		const size_t l_begin = l_off;
+		for (uint32_t k = 0; k != gn; ++k) {
+			const risltc_batch_item_t& it = items[g0 + k];
+			const uint32_t np = it.gbuffer.width * it.gbuffer.height;
+			const uint32_t pf = np * it.frame_count;
+			Scratch sc{};
+			sc.records = ctx->d_records + r_off;
+			sc.p_hat = ctx->d_phat;
+			sc.samples = ctx->d_samples + w_off;
+			sc.staged = ctx->d_staged + 2 * w_off;
+			sc.rays = ctx->d_rays + 2 * w_off;
+			sc.hits = ctx->d_hits + 2 * w_off;
+			sc.ray_count = ctx->d_ray_count + 2 * (size_t) (g0 + k);
+			sc.light_rays = ctx->d_light_rays + l_off * risltc::kLightCounterStride;
+			b.item[k] = ris_params(ctx, sc, it.scene, &it.gbuffer, &it.settings, it.noise->random_seed, it.animate,
+			                       it.frame_count, it.out_rgb, it.accum, it.reservoirs, true);
+			b.tile_begin[k] = tiles;
+			b.pixel_begin[k] = pixels;
+			b.pf_begin[k] = pfs;
+			tiles += (np + px_per_tile - 1) / px_per_tile;
+			pixels += np;
+			pfs += pf;
+			r_off += pf;
+			w_off += pf;
+			l_off += (size_t) it.scene->view.light_count;
+		}
+		b.tile_begin[gn] = tiles;
+		b.pixel_begin[gn] = pixels;
+		b.pf_begin[gn] = pfs;
+		cudaError_t e = cudaMemsetAsync(ctx->d_light_rays + l_begin * risltc::kLightCounterStride, 0,
+		                                sizeof(uint32_t) * (l_off - l_begin) * risltc::kLightCounterStride, ctx->stream);
+		if (e == cudaSuccess)
+			e = fast ? risltc::launch_candidates_batch_fast(b, ctx->stream, ctx->sm_count * 16, (int) tile)
+			         : risltc::launch_candidates_batch_exact(b, ctx->stream, ctx->sm_count * 16, (int) tile);
+		if (e == cudaSuccess)
+			e = risltc::launch_batch_estimator(b, ctx->stream, grid_for(ctx, pixels), grid_for(ctx, pfs),
+			                                   grid_for(ctx, 2 * (size_t) pfs));
+		if (e != cudaSuccess) return cuda_status(e);
+		ctx->kernel_launches += 6;
+	}
+	for (uint32_t i = 0; i != item_count; ++i) items[i].noise->random_seed += items[i].frame_count;
+	return RISLTC_OK;
+}
+
+}  // namespace
+
 EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* items, uint32_t item_count) {
 	if (!ctx || (!items && item_count)) return RISLTC_ERROR_INVALID_ARGUMENT;
 	if (item_count == 0) return RISLTC_OK;
@@ -1086,7 +1194,9 @@ EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* it
 	if (records && (st = reserve_phat(ctx, RISLTC_BATCH_STREAMS))) return st;
 	if (candidates && (st = reserve_candidates(ctx, candidates))) return st;
 	if (logits && (st = reserve_logits(ctx, logits))) return st;
-	if (queues && (st = reserve_wavefront(ctx, wavefront, lights, queues))) return st;
+	// One more queue slot than items: the whole-batch trace's fetch cursor.
+	if (queues && (st = reserve_wavefront(ctx, wavefront, lights, queues + 1))) return st;
+	if (batch_is_fused(items, item_count)) return shade_batch_fused(ctx, items, item_count, queues);
 	cudaError_t e = cudaSuccess;
 	if (!ctx->batch_streams_created) {
 		e = cudaEventCreateWithFlags(&ctx->batch_fork, cudaEventDisableTiming);

@@ -334,24 +334,21 @@ RL_DEV bool evaluate_candidate(const float* f, const float4* record, bool allow_
 #endif
 }
 
+// One warp tile t (pixels t * kPixels .. + kPixels - 1) of one frame set:
+// candidates, evaluation, replay and reservoir records for all frames.
+// tile is the warp's shared-memory tile, phat its p_hat slot.
 template <class P, int kPixels, int kChunk>
-__global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
-ris_candidates_binned_kernel(RisParams pr) {
-	extern __shared__ __align__(16) unsigned char smem_raw[];
+RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPixels, kChunk>& tile, float* phat,
+                        uint32_t t) {
 	constexpr int kSuper = BinnedSuper<P>::value;
-	using Tile = WarpTile<kSuper, kPixels, kChunk>;
-	Tile& tile = reinterpret_cast<Tile*>(smem_raw)[threadIdx.x / 32];
-	float* const phat = pr.p_hat_scratch + (size_t) (blockIdx.x * kBinnedWarps + threadIdx.x / 32) * kPHatSlot;
 	const uint32_t lane = threadIdx.x % 32;
 	const uint32_t np = pr.width * pr.height;
 	const int n_lights = pr.scene.light_count;
 	const float p = P::rcp((float) n_lights);
-	const uint32_t warps_total = gridDim.x * kBinnedWarps;
-	const uint32_t tiles = (np + kPixels - 1) / kPixels;
 	// Lanes kPixels..31 own no pixel: they draw nothing and only evaluate
 	// items of the sorted lists.
 	const bool own = lane < (uint32_t) kPixels;
-	for (uint32_t t = blockIdx.x * kBinnedWarps + threadIdx.x / 32; t < tiles; t += warps_total) {
+	{
 		const uint32_t i = t * kPixels + lane;
 		const bool valid = own && i < np && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
 		if (valid) {
@@ -519,6 +516,18 @@ ris_candidates_binned_kernel(RisParams pr) {
 		}
 		__syncwarp();
 	}
+}
+
+template <class P, int kPixels, int kChunk>
+__global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
+ris_candidates_binned_kernel(const __grid_constant__ RisParams pr) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	using Tile = WarpTile<BinnedSuper<P>::value, kPixels, kChunk>;
+	Tile& tile = reinterpret_cast<Tile*>(smem_raw)[threadIdx.x / 32];
+	float* const phat = pr.p_hat_scratch + (size_t) (blockIdx.x * kBinnedWarps + threadIdx.x / 32) * kPHatSlot;
+	const uint32_t tiles = (pr.width * pr.height + kPixels - 1) / kPixels;
+	for (uint32_t t = blockIdx.x * kBinnedWarps + threadIdx.x / 32; t < tiles; t += gridDim.x * kBinnedWarps)
+		binned_tile<P, kPixels, kChunk>(pr, tile, phat, t);
 }
 
 template <class P, int kPixels, int kChunk> constexpr size_t binned_smem_bytes() {

@@ -173,7 +173,9 @@ RL_DEV void store_sample(SampleRecord* dst, const f3 (&c)[2][2], float W, uint32
 #ifndef RISLTC_SAMPLE_MIN_BLOCKS
 #define RISLTC_SAMPLE_MIN_BLOCKS 4
 #endif
-template <class P> __global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_kernel(RisParams pr) {
+// The sample phase of pixel i (all frames of the call); i may be past the
+// frame (the thread then does nothing).
+template <class P> RL_DEV void sample_pixel(const RisParams& pr, uint32_t i) {
 	const uint32_t np = pr.width * pr.height;
 	ShadeParams sp;  // the fields psa_prepare_both and psa_mis_emit read
 	sp.scene = pr.scene;
@@ -184,8 +186,7 @@ template <class P> __global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOC
 	sp.fast_atan = pr.fast_atan;
 	sp.shadows = pr.shadows;
 	sp.error = pr.error;
-	for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x) {
-		const uint32_t i = base + threadIdx.x;
+	{
 		const bool active = i < np && !(pr.primitive && pr.primitive[i] == 0xffffffffu);
 		ShadingData sd;
 		Ltc ltc;
@@ -232,12 +233,19 @@ template <class P> __global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOC
 	}
 }
 
+template <class P>
+__global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_kernel(const __grid_constant__ RisParams pr) {
+	const uint32_t np = pr.width * pr.height;
+	for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x)
+		sample_pixel<P>(pr, base + threadIdx.x);
+}
+
 // Exclusive prefix sum of the per-light ray counts, in place (each becomes
 // its bucket's first queue position); the total goes to ray_count[0] and the
 // trace kernel's fetch cursor ray_count[1] is reset.  One block of 1024
 // threads.
-static __global__ void __launch_bounds__(1024) light_bucket_scan_kernel(uint32_t* light_rays, uint32_t light_count,
-                                                                 uint32_t* ray_count) {
+// The scan by one block of 1024 threads.
+RL_DEV void light_bucket_scan(uint32_t* light_rays, uint32_t light_count, uint32_t* ray_count) {
 	__shared__ uint32_t warp_offset[32];
 	__shared__ uint32_t chunk_total;
 	const uint32_t lane = threadIdx.x % 32, warp = threadIdx.x / 32;
@@ -274,19 +282,23 @@ static __global__ void __launch_bounds__(1024) light_bucket_scan_kernel(uint32_t
 		ray_count[1] = 0;  // the trace kernel's fetch cursor
 	}
 }
+static __global__ void __launch_bounds__(1024) light_bucket_scan_kernel(uint32_t* light_rays, uint32_t light_count,
+                                                                 uint32_t* ray_count) {
+	light_bucket_scan(light_rays, light_count, ray_count);
+}
 
 // Moves the staged rays into their light's bucket, tagging each with its hit
 // slot.
-static __global__ void __launch_bounds__(128) shadow_scatter_kernel(RisParams pr) {
+// The staged rays of pixel-frame pf into their light's bucket.
+RL_DEV void scatter_pixel_frame(const RisParams& pr, size_t pf) {
 	const uint32_t np = pr.width * pr.height;
-	const size_t total = (size_t) np * pr.frame_count;
-	for (size_t pf = blockIdx.x * (size_t) blockDim.x + threadIdx.x; pf < total; pf += (size_t) gridDim.x * blockDim.x) {
+	{
 		const uint32_t i = (uint32_t) (pf % np);
-		if (pr.primitive && pr.primitive[i] == 0xffffffffu) continue;
+		if (pr.primitive && pr.primitive[i] == 0xffffffffu) return;
 		const uint32_t flags = __float_as_uint(reinterpret_cast<const float4*>(pr.samples + pf)[3].y);
-		if (flags & kSampleNoLight) continue;
+		if (flags & kSampleNoLight) return;
 		const bool t0 = (flags & 3u) == kSampleTraced, t1 = ((flags >> 2) & 3u) == kSampleTraced;
-		if (!t0 && !t1) continue;
+		if (!t0 && !t1) return;
 		uint32_t at = atomicAdd(pr.light_rays + (size_t) pr.records[pf].light_index * kLightCounterStride,
 		                        (t0 ? 1u : 0u) + (t1 ? 1u : 0u));
 		const uint32_t slot = 2u * (uint32_t) pf;
@@ -301,6 +313,11 @@ static __global__ void __launch_bounds__(128) shadow_scatter_kernel(RisParams pr
 			pr.rays[at] = q;
 		}
 	}
+}
+static __global__ void __launch_bounds__(128) shadow_scatter_kernel(const __grid_constant__ RisParams pr) {
+	const size_t total = (size_t) pr.width * pr.height * pr.frame_count;
+	for (size_t pf = blockIdx.x * (size_t) blockDim.x + threadIdx.x; pf < total; pf += (size_t) gridDim.x * blockDim.x)
+		scatter_pixel_frame(pr, pf);
 }
 
 #ifndef RISLTC_TRACE_MIN_BLOCKS
@@ -356,9 +373,10 @@ __global__ void __launch_bounds__(128, RISLTC_TRACE_MIN_BLOCKS) shadow_trace_ker
 	}
 }
 
-template <class P> __global__ void __launch_bounds__(128) ris_resolve_kernel(RisParams pr) {
+// The resolve phase of pixel i (all frames of the call).
+template <class P> RL_DEV void resolve_pixel(const RisParams& pr, uint32_t i) {
 	const uint32_t np = pr.width * pr.height;
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+	{
 		risltc_reservoir_t* res = pr.reservoirs ? pr.reservoirs + i : nullptr;
 		if (pr.primitive && pr.primitive[i] == 0xffffffffu) {
 			if (res) *res = risltc_reservoir_t{-1, 0.0f, 0.0f, 0u};
@@ -367,7 +385,7 @@ template <class P> __global__ void __launch_bounds__(128) ris_resolve_kernel(Ris
 				pr.out_rgb[3 * (size_t) i + 1] = 0.0f;
 				pr.out_rgb[3 * (size_t) i + 2] = 0.0f;
 			}
-			continue;
+			return;
 		}
 		f3 sum = splat(0.0f);
 		double acc[3] = {0.0, 0.0, 0.0};
@@ -419,6 +437,12 @@ template <class P> __global__ void __launch_bounds__(128) ris_resolve_kernel(Ris
 			pr.accum[3 * (size_t) i + 2] += acc[2];
 		}
 	}
+}
+
+template <class P> __global__ void __launch_bounds__(128) ris_resolve_kernel(const __grid_constant__ RisParams pr) {
+	const uint32_t np = pr.width * pr.height;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+		resolve_pixel<P>(pr, i);
 }
 
 }  // namespace risltc

@@ -2,8 +2,7 @@
 // root: everything that must match the CPU restatement bit for bit, plus the
 // fused kernel's fast-candidate variant (its candidate loop uses hardware
 // reciprocal square root; its final shading stays exact).
-#include "ris_binned.cuh"
-#include "ris_wavefront.cuh"
+#include "ris_batch.cuh"
 
 namespace risltc {
 cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast) {
@@ -51,6 +50,23 @@ cudaError_t launch_shadow_trace(const RisParams& p, cudaStream_t stream, int gri
 }
 cudaError_t launch_ris_resolve(const RisParams& p, cudaStream_t stream, int grid) {
 	ris_resolve_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	return cudaGetLastError();
+}
+cudaError_t launch_candidates_batch_exact(const RisBatch& b, cudaStream_t stream, int grid_cap, int tile) {
+	if (tile == risltc_tile_32x8) return launch_candidates_batch<ExactNumerics, 32, 8>(b, stream, grid_cap);
+	return launch_candidates_batch_tile_exact(b, stream, grid_cap, tile);
+}
+cudaError_t launch_batch_estimator(const RisBatch& b, cudaStream_t stream, int pixel_grid, int pf_grid, int ray_grid) {
+	ris_sample_batch_kernel<ExactNumerics><<<pixel_grid, 128, 0, stream>>>(b);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	light_bucket_scan_batch_kernel<<<b.count, 1024, 0, stream>>>(b);
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	shadow_scatter_batch_kernel<<<pf_grid, 128, 0, stream>>>(b);
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	shadow_trace_batch_kernel<ExactNumerics><<<ray_grid, 128, 0, stream>>>(b);
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	ris_resolve_batch_kernel<ExactNumerics><<<pixel_grid, 128, 0, stream>>>(b);
 	return cudaGetLastError();
 }
 cudaError_t launch_trace_exact(const SceneView& s, const float4* rays, uint32_t count, uint32_t* hits, uint32_t* error,

@@ -1,7 +1,7 @@
 // Fast-numerics candidate kernel: hardware reciprocal square root,
 // approximate division and contraction of multiply-add (--fmad=true) in the
 // RIS candidate loop, whose results only weight the reservoir.
-#include "ris_binned.cuh"
+#include "ris_batch.cuh"
 
 namespace risltc {
 cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int grid_cap, int tile) {
@@ -12,5 +12,9 @@ cudaError_t launch_candidates_fast(const RisParams& p, cudaStream_t stream, int 
 		return cudaGetLastError();
 	}
 	return launch_candidates_tile_fast(p, stream, grid_cap, tile);
+}
+cudaError_t launch_candidates_batch_fast(const RisBatch& b, cudaStream_t stream, int grid_cap, int tile) {
+	if (tile == risltc_tile_32x8) return launch_candidates_batch<FastNumerics, 32, 8>(b, stream, grid_cap);
+	return launch_candidates_batch_tile_fast(b, stream, grid_cap, tile);
 }
 }  // namespace risltc

@@ -80,3 +80,68 @@ def test_batch_rejects_a_bad_item_before_any_work(gpu):
     assert torch.all(out == -1.0)
     sc.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("tile", ["32x8", "16x4"])
+def test_whole_batch_launches_equal_single_calls(gpu, tile):
+    """20 shadowed frames of mixed sizes, light and occluder counts in the
+    default configuration: risltc_shade_batch runs one launch per phase for
+    each group of 16 items (6 kernels per group, counted by the context), and
+    every item's image, FP64 sums and reservoirs equal its own risltc_shade
+    call bit for bit, also when replayed from a captured graph."""
+    import torch
+    import risltc_gb300 as rl
+    rng = np.random.default_rng(9)
+    hss = []
+    for i in range(20):
+        w = int(np.exp(rng.uniform(np.log(24), np.log(160))))
+        h = int(np.exp(rng.uniform(np.log(16), np.log(96))))
+        lights = int(np.exp(rng.uniform(np.log(16), np.log(512))))
+        tris = int(np.exp(rng.uniform(np.log(300), np.log(5000))))
+        hss.append(rl.scenes.plane_of_quads(w, h, lights, seed=900 + i, triangles=tris))
+    stream = torch.cuda.Stream()
+    ctx = rl.Context(0, stream=stream.cuda_stream)
+    scenes = [rl.Scene.from_host_scene(ctx, hs) for hs in hss]
+    s = rl.settings(candidates=8, tile=tile)
+    items, singles = [], []
+    with torch.cuda.stream(stream):
+        for k, (hs, sc) in enumerate(zip(hss, scenes)):
+            g = torch.from_numpy(hs.gbuffer).cuda()
+            frames = 1 + k % 2
+            want = (torch.zeros((hs.pixels, 3), dtype=torch.float32, device="cuda"),
+                    torch.zeros((hs.pixels, 3), dtype=torch.float64, device="cuda"),
+                    torch.zeros((hs.pixels, 4), dtype=torch.int32, device="cuda"))
+            rl.shade(ctx, sc, g, hs.width, hs.height, s, noise_seed=11 * k, frames=frames, out_rgb=want[0],
+                     accum=want[1], reservoirs=want[2])
+            singles.append(want)
+            items.append(dict(scene=sc, gbuffer=g, width=hs.width, height=hs.height, settings=s, noise_seed=11 * k,
+                              frames=frames, out_rgb=torch.full((hs.pixels, 3), -1.0, device="cuda"),
+                              accum=torch.zeros((hs.pixels, 3), dtype=torch.float64, device="cuda"),
+                              reservoirs=torch.zeros((hs.pixels, 4), dtype=torch.int32, device="cuda")))
+        before = ctx.launch_count()
+        seeds = rl.shade_batch(ctx, items)
+        assert ctx.launch_count() - before == 2 * 6
+    ctx.check()
+    assert seeds == [11 * k + 1 + k % 2 for k in range(len(items))]
+
+    def check():
+        for it, (rgb, acc, res) in zip(items, singles):
+            assert torch.equal(it["out_rgb"], rgb)
+            assert torch.equal(it["accum"], acc)
+            assert torch.equal(it["reservoirs"], res)
+    check()
+    for it in items:
+        it["out_rgb"].fill_(-1.0)
+        it["accum"].zero_()
+        it["reservoirs"].zero_()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        rl.shade_batch(ctx, items)
+    graph.replay()
+    torch.cuda.synchronize()
+    ctx.check()
+    check()
+    for sc in scenes:
+        sc.close()
+    ctx.close()
