@@ -511,14 +511,20 @@ typedef struct risltc_batch_item_s {
 
 /* Shades several G-buffers (each with its own scene, settings and noise) in
  * one call; no counterpart in the reference, which draws one view at a time.
- * Each item gets its own share of the context's scratch and runs on one of
- * RISLTC_BATCH_STREAMS streams forked from the context's stream and joined
- * back to it, so that small frames fill the GPU together.  Results equal the
- * items' risltc_shade calls bit for bit.  All items are validated before any
- * work; noise->random_seed of each item advances by its frame_count.  The
- * first call grows the scratch and creates the streams; later calls with no
- * larger items allocate nothing, so a batch can be captured into one CUDA
- * graph. */
+ * Each item gets its own share of the context's scratch.  When every item
+ * uses the default configuration (LTC-CP, light_reservoir, one light sample
+ * and one sample per technique, uniform candidates, shadows on a scene with
+ * occluders) with the same numerics and a binned tile shape, the batch runs
+ * as one launch per phase for all items (candidate, sample, ray grouping,
+ * trace and resolve kernels over the items' concatenated work, in groups of
+ * 16 items) on the context's stream; otherwise each item runs its own
+ * kernels on one of RISLTC_BATCH_STREAMS streams forked from the context's
+ * stream and joined back to it.  Either way small frames fill the GPU
+ * together and the results equal the items' risltc_shade calls bit for bit.
+ * All items are validated before any work; noise->random_seed of each item
+ * advances by its frame_count.  The first call grows the scratch (and creates
+ * the streams where needed); later calls with no larger items allocate
+ * nothing, so a batch can be captured into one CUDA graph. */
 EXTERN_C int risltc_shade_batch(risltc_ctx_t* ctx, const risltc_batch_item_t* items, uint32_t item_count);
 
 /* Autotuner of the candidate kernel's tile shape: for every risltc_tile_t,

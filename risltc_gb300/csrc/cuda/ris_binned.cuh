@@ -207,8 +207,26 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 #endif
 constexpr int kPairUnroll = RISLTC_PAIR_UNROLL;
 
-RL_DEV float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-RL_DEV float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// Paired add and multiply as PTX with an explicit rounding modifier: the
+// code generator never contracts such instructions into fused multiply-adds
+// (the __fadd2_rn / __fmul2_rn intrinsics were contracted into FFMA2 even
+// with --fmad=false, which changes the rounding of exact numerics).
+RL_DEV float2 add2(float2 a, float2 b) {
+	float2 d;
+	asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+	    "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+	    : "=f"(d.x), "=f"(d.y)
+	    : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+	return d;
+}
+RL_DEV float2 mul2(float2 a, float2 b) {
+	float2 d;
+	asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+	    "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+	    : "=f"(d.x), "=f"(d.y)
+	    : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+	return d;
+}
 RL_DEV float2 pair(float a) { return make_float2(a, a); }
 // a * b + c, contracted in fast numerics.
 template <class P> RL_DEV float2 mad2(float2 a, float2 b, float2 c) { return add2(mul2(a, b), c); }
@@ -267,24 +285,36 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 		t.c[c].y = make_float2(ms[3 * c + 1], mc[3 * c + 1]);
 		t.c[c].z = make_float2(ms[3 * c + 2], mc[3 * c + 2]);
 	}
-	float4 q = __ldg(record + 2);
-	f3x2 v = mul_point2<P>(t, q);
+	// Vertices 0 and 1 first; then iteration j normalises vertex j + 1 while
+	// it integrates edge (j - 1, j), so the two dependency chains overlap.
+	// The edges are added in calculate_ltc's order: (0, 1), ..., (n - 2,
+	// n - 1), then (n - 1, 0).
+	const float4 q0 = __ldg(record + 2), q1 = __ldg(record + 3);
+	float4 q = __ldg(record + 4);
+	f3x2 v = mul_point2<P>(t, q0);
 	if (flip) v.y.x = -v.y.x;
-	q = __ldg(record + 3);
 	uint32_t above_s = v.z.x > 0.0f ? 1u : 0u, above_c = v.z.y > 0.0f ? 1u : 0u;
 	const f3x2 first = normalize2<P>(v);
-	f3x2 prev = first;
+	v = mul_point2<P>(t, q1);
+	if (flip) v.y.x = -v.y.x;
+	above_s += v.z.x > 0.0f ? 1u : 0u;
+	above_c += v.z.y > 0.0f ? 1u : 0u;
+	f3x2 prev = first, cur = normalize2<P>(v);
 	float2 r = pair(0.0f);
 #pragma unroll kPairUnroll
 	for (uint32_t j = 1; j != n; ++j) {
-		v = mul_point2<P>(t, q);
-		if (flip) v.y.x = -v.y.x;
-		q = __ldg(record + 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
-		above_s += v.z.x > 0.0f ? 1u : 0u;
-		above_c += v.z.y > 0.0f ? 1u : 0u;
-		const f3x2 cur = normalize2<P>(v);
+		f3x2 next = first;
+		if (j + 1 != n) {
+			v = mul_point2<P>(t, q);
+			if (flip) v.y.x = -v.y.x;
+			q = __ldg(record + 2 + min(j + 2, (uint32_t) kMaxLightVertices - 1));
+			above_s += v.z.x > 0.0f ? 1u : 0u;
+			above_c += v.z.y > 0.0f ? 1u : 0u;
+			next = normalize2<P>(v);
+		}
 		r = add2(r, integrate_edge2<P>(prev, cur));
 		prev = cur;
+		cur = next;
 	}
 	r = add2(r, integrate_edge2<P>(prev, first));
 	const bool partial_s = above_s != n && above_s != 0, partial_c = above_c != n && above_c != 0;
