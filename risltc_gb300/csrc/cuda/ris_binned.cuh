@@ -207,10 +207,22 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 #endif
 constexpr int kPairUnroll = RISLTC_PAIR_UNROLL;
 
-// Paired add and multiply as PTX with an explicit rounding modifier: the
-// code generator never contracts such instructions into fused multiply-adds
-// (the __fadd2_rn / __fmul2_rn intrinsics were contracted into FFMA2 even
-// with --fmad=false, which changes the rounding of exact numerics).
+// The paired operations.  Fast numerics uses the paired instructions
+// (FADD2 / FMUL2 / FFMA2), which the code generator may contract into fused
+// multiply-adds.  Exact numerics must not be contracted, and the code
+// generator contracts a paired multiply followed by a paired add into FFMA2
+// even with --fmad=false and explicit rounding modifiers (measured: every
+// exact-numerics frame then differed from the oracle).  So by default exact
+// numerics computes each lane with its own correctly rounded scalar
+// operation (__fadd_rn / __fmul_rn, never contracted); the loop still
+// carries both spaces' independent dependency chains side by side.
+// RISLTC_PAIR_OPS selects the form for exact numerics: 0 scalar per lane,
+// 1 paired PTX add/mul, 2 paired fused multiply-adds with exact one and
+// zero operands (RN(a * b + -0) = RN(a * b), RN(a * 1 + b) = RN(a + b)).
+#ifndef RISLTC_PAIR_OPS
+#define RISLTC_PAIR_OPS 0
+#endif
+#if RISLTC_PAIR_OPS == 1
 RL_DEV float2 add2(float2 a, float2 b) {
 	float2 d;
 	asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
@@ -227,10 +239,35 @@ RL_DEV float2 mul2(float2 a, float2 b) {
 	    : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
 	return d;
 }
+#elif RISLTC_PAIR_OPS == 2
+RL_DEV float2 add2(float2 a, float2 b) { return __ffma2_rn(a, make_float2(1.0f, 1.0f), b); }
+RL_DEV float2 mul2(float2 a, float2 b) { return __ffma2_rn(a, b, make_float2(-0.0f, -0.0f)); }
+#else
+RL_DEV float2 add2(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+RL_DEV float2 mul2(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+#endif
+// Fast numerics: the paired instructions, contraction allowed.
+struct PairFast {
+	static RL_DEV float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+	static RL_DEV float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+	static RL_DEV float2 mad(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+};
+struct PairExact {
+	static RL_DEV float2 add(float2 a, float2 b) { return add2(a, b); }
+	static RL_DEV float2 mul(float2 a, float2 b) { return mul2(a, b); }
+	static RL_DEV float2 mad(float2 a, float2 b, float2 c) { return add2(mul2(a, b), c); }
+};
+template <class P> struct PairOps {
+	using type = PairExact;
+};
+template <> struct PairOps<FastNumerics> {
+	using type = PairFast;
+};
 RL_DEV float2 pair(float a) { return make_float2(a, a); }
-// a * b + c, contracted in fast numerics.
-template <class P> RL_DEV float2 mad2(float2 a, float2 b, float2 c) { return add2(mul2(a, b), c); }
-template <> RL_DEV float2 mad2<FastNumerics>(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a * b + c (contracted in fast numerics), a + b and a * b in both lanes.
+template <class P> RL_DEV float2 mad2(float2 a, float2 b, float2 c) { return PairOps<P>::type::mad(a, b, c); }
+template <class P> RL_DEV float2 padd(float2 a, float2 b) { return PairOps<P>::type::add(a, b); }
+template <class P> RL_DEV float2 pmul(float2 a, float2 b) { return PairOps<P>::type::mul(a, b); }
 
 struct f3x2 {
 	float2 x, y, z;
@@ -242,30 +279,30 @@ struct mat43x2 {
 template <class P> RL_DEV f3x2 mul_point2(const mat43x2& m, float4 q) {
 	const float2 px = pair(q.x), py = pair(q.y), pz = pair(q.z);
 	f3x2 r;
-	r.x = add2(mad2<P>(m.c[2].x, pz, mad2<P>(m.c[1].x, py, mul2(m.c[0].x, px))), m.c[3].x);
-	r.y = add2(mad2<P>(m.c[2].y, pz, mad2<P>(m.c[1].y, py, mul2(m.c[0].y, px))), m.c[3].y);
-	r.z = add2(mad2<P>(m.c[2].z, pz, mad2<P>(m.c[1].z, py, mul2(m.c[0].z, px))), m.c[3].z);
+	r.x = padd<P>(mad2<P>(m.c[2].x, pz, mad2<P>(m.c[1].x, py, pmul<P>(m.c[0].x, px))), m.c[3].x);
+	r.y = padd<P>(mad2<P>(m.c[2].y, pz, mad2<P>(m.c[1].y, py, pmul<P>(m.c[0].y, px))), m.c[3].y);
+	r.z = padd<P>(mad2<P>(m.c[2].z, pz, mad2<P>(m.c[1].z, py, pmul<P>(m.c[0].z, px))), m.c[3].z);
 	return r;
 }
 template <class P> RL_DEV float2 dot2(const f3x2& a, const f3x2& b) {
-	return mad2<P>(a.z, b.z, mad2<P>(a.y, b.y, mul2(a.x, b.x)));
+	return mad2<P>(a.z, b.z, mad2<P>(a.y, b.y, pmul<P>(a.x, b.x)));
 }
 template <class P> RL_DEV f3x2 normalize2(const f3x2& a) {
 	const float2 d = dot2<P>(a, a);
 	const float2 s = make_float2(P::rsqrt(d.x), P::rsqrt(d.y));
-	return {mul2(a.x, s), mul2(a.y, s), mul2(a.z, s)};
+	return {pmul<P>(a.x, s), pmul<P>(a.y, s), pmul<P>(a.z, s)};
 }
 // integrate_edge on both lanes.
 template <class P> RL_DEV float2 integrate_edge2(const f3x2& v1, const f3x2& v2) {
 	const float2 x = dot2<P>(v1, v2);
 	const float2 y = make_float2(fabsf(x.x), fabsf(x.y));
-	const float2 a = add2(pair(0.8543985f), mul2(mad2<P>(pair(0.0145206f), y, pair(0.4965155f)), y));
-	const float2 b = add2(pair(3.4175940f), mul2(add2(pair(4.1616724f), y), y));
+	const float2 a = padd<P>(pair(0.8543985f), pmul<P>(mad2<P>(pair(0.0145206f), y, pair(0.4965155f)), y));
+	const float2 b = padd<P>(pair(3.4175940f), pmul<P>(padd<P>(pair(4.1616724f), y), y));
 	float2 ts = make_float2(P::div(a.x, b.x), P::div(a.y, b.y));
 	if (!(x.x > 0.0f)) ts.x = 0.5f * P::rsqrt(fmax_glsl(1.0f - x.x * x.x, 1e-7f)) - ts.x;
 	if (!(x.y > 0.0f)) ts.y = 0.5f * P::rsqrt(fmax_glsl(1.0f - x.y * x.y, 1e-7f)) - ts.y;
-	const float2 cz = add2(mul2(v1.x, v2.y), mul2(make_float2(-v1.y.x, -v1.y.y), v2.x));
-	return mul2(cz, ts);
+	const float2 cz = padd<P>(pmul<P>(v1.x, v2.y), pmul<P>(make_float2(-v1.y.x, -v1.y.y), v2.x));
+	return pmul<P>(cz, ts);
 }
 
 template <class P>
@@ -312,11 +349,11 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 			above_c += v.z.y > 0.0f ? 1u : 0u;
 			next = normalize2<P>(v);
 		}
-		r = add2(r, integrate_edge2<P>(prev, cur));
+		r = padd<P>(r, integrate_edge2<P>(prev, cur));
 		prev = cur;
 		cur = next;
 	}
-	r = add2(r, integrate_edge2<P>(prev, first));
+	r = padd<P>(r, integrate_edge2<P>(prev, first));
 	const bool partial_s = above_s != n && above_s != 0, partial_c = above_c != n && above_c != 0;
 	if ((partial_s || partial_c) && !allow_clip) return false;
 	float integral[2];
