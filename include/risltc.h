@@ -388,8 +388,10 @@ EXTERN_C int risltc_model_set_training(risltc_model_t* model, int enable, float 
    part needs shadows on and one sample per technique. */
 EXTERN_C int risltc_model_set_target_mix(risltc_model_t* model, float shadowed_weight);
 /* How training steps run (flags, default 0): on the tensor cores (tcgen05,
-   BF16 operands, FP32 accumulation) for models of up to 256 clusters, in
-   FP32 on the CUDA cores beyond that.  RISLTC_TRAIN_CUDA_CORES: the FP32
+   BF16 operands, FP32 accumulation) for every model (up to 256 clusters with
+   all weight gradients accumulated in tensor memory, beyond that with the
+   output layer in chunks of 128 clusters whose weight gradients are added to
+   the gradient vector per tile).  RISLTC_TRAIN_CUDA_CORES: the FP32
    CUDA-core kernel for every model.  RISLTC_TRAIN_ACCUMULATE_ONLY: each
    training call adds its gradient to the model's gradient vector and takes
    no Adam step (risltc_model_apply_update takes it). */

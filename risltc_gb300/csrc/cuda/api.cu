@@ -11,6 +11,7 @@
 #include "mlp.cuh"
 #include "mlp_tc.cuh"
 #include "mlp_train_tc.cuh"
+#include "mlp_train_tc_wide.cuh"
 #include "ris_batch.cuh"
 
 // Triangles per BVH leaf before the SAH is consulted.
@@ -647,6 +648,9 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 		if (e == cudaSuccess)
 			e = cudaFuncSetAttribute(risltc::mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			                         (int) risltc::kTtSmemBytes);
+		if (e == cudaSuccess)
+			e = cudaFuncSetAttribute(risltc::mlp_train_tc_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                         (int) risltc::kTwSmemBytes);
 		if (e != cudaSuccess) return e;
 		configured.fetch_or(bit);
 	}
@@ -657,6 +661,13 @@ cudaError_t launch_training(risltc_ctx_t* ctx, cudaStream_t stream, const risltc
 		const int blocks = (int) std::min<uint32_t>((n_train + risltc::kTcRows - 1) / risltc::kTcRows,
 		                                            (uint32_t) ctx->sm_count);
 		risltc::mlp_train_tc_kernel<<<blocks, risltc::kTcThreads, risltc::kTtSmemBytes, stream>>>(t);
+	} else if (m->cluster_count <= risltc::kTwMaxClusters && !(m->training_flags & RISLTC_TRAIN_CUDA_CORES)) {
+		// More than 256 clusters: the output layer in chunks of 128.
+		t.skip_issue = (ctx->inject & RISLTC_FAULT_TRAIN_TENSOR_WAIT) ? 1u : 0u;
+		ctx->inject &= ~(uint32_t) RISLTC_FAULT_TRAIN_TENSOR_WAIT;
+		const int blocks = (int) std::min<uint32_t>((n_train + risltc::kTcRows - 1) / risltc::kTcRows,
+		                                            (uint32_t) ctx->sm_count);
+		risltc::mlp_train_tc_wide_kernel<<<blocks, risltc::kTcThreads, risltc::kTwSmemBytes, stream>>>(t);
 	} else {
 		// Two blocks per SM where their shared memory fits (up to about 500
 		// clusters), one otherwise.

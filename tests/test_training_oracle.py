@@ -8,7 +8,8 @@ gradient (checked against finite differences of the loss on the CPU below):
 the FP32 CUDA-core kernel against the unrounded gradient, the tcgen05 kernel
 against the same gradient with the kernel's BF16 roundings (features,
 weights, activations, logits and logit gradients).  Cases: 8, 72 and 256
-clusters, an odd candidate count, invalid and zero-weight candidates,
+clusters (all weight gradients in tensor memory), 520 and 1024 clusters (the
+output layer in chunks of 128, a partial last chunk at 520), an odd candidate count, invalid and zero-weight candidates,
 background pixels, a training stride that leaves a partial last 128-pixel
 tile, with and without the shadowed target part.  The training signal
 replaces the reference's uniform candidate pdf p = 1/N
@@ -76,7 +77,7 @@ def test_oracle_gradient_equals_finite_differences():
 def setup(gpu):
     import torch
     import risltc_gb300 as rl
-    hs0 = rl.scenes.heightfield(150, 90, light_count=600, triangle_count=0, seed=9, vertex_counts=(3, 8))
+    hs0 = rl.scenes.heightfield(150, 90, light_count=2400, triangle_count=0, seed=9, vertex_counts=(3, 8))
     ctx = rl.Context(0)
     yield rl, torch, ctx, hs0
     ctx.close()
@@ -84,7 +85,8 @@ def setup(gpu):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("k,m,stride,phase,shadowed", [(8, 13, 3, 1, True), (72, 7, 5, 2, False),
-                                                       (256, 32, 3, 0, True)])
+                                                       (256, 32, 3, 0, True), (520, 11, 3, 1, True),
+                                                       (1024, 32, 2, 0, False)])
 def test_training_gradient_matches_oracle(setup, k, m, stride, phase, shadowed):
     rl, torch, ctx, hs0 = setup
     hs, offsets = rl.scenes.cluster_lights(hs0, k, seed=3)
