@@ -573,11 +573,11 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 						}
 						const float rnd = get_noise_1(seed);
 						const float p_hat = phat[lane * kSuper + k];
-						const float w = P::div(p_hat, pk);
+						const float w = P::div_moderate(p_hat, pk);
 						if (pr.train_stride && f == 0 && i % pr.train_stride == pr.train_phase)
 							pr.train_candidates[(size_t) i * pr.candidate_count + cs + k].pdf = w;
 						w_sum += w;
-						if (w > 0.0f && rnd < P::div(w, w_sum)) {
+						if (w > 0.0f && rnd < P::div_moderate(w, w_sum)) {
 							res_index = idx;
 							sample_value = p_hat;
 						}

@@ -2,7 +2,7 @@
 // shade_device.cuh (sqrt_markstein, rcp_markstein, div_markstein) against
 // CUDA's correctly rounded intrinsics, on this GPU's approximation units.
 //
-// risltc_test_markstein(counts) fills counts[6]:
+// risltc_test_markstein(counts) fills counts[7]:
 //   0 square roots differing from __fsqrt_rn over every positive normal float;
 //   1 reciprocals differing from __frcp_rn over every float in [2^-126, 2^126);
 //   2 reciprocal square roots rcp(sqrt(x)) differing from
@@ -10,7 +10,10 @@
 //   3 reciprocals differing over every divisor in [2, 16);
 //   4 quotients differing from __fdiv_rn for every divisor in [2, 16) with
 //     eight numerators each, spread over [0.5, 2);
-//   5 the number of quotients checked.
+//   5 the number of quotients checked;
+//   6 quotients differing from __fdiv_rn over 2^28 pseudo-random pairs whose
+//     magnitudes span [2^-60, 2^60] (either sign), the operand range of
+//     ExactNumerics::div_moderate.
 // Returns a cudaError_t.
 #include <cuda_runtime.h>
 
@@ -53,19 +56,37 @@ __global__ void markstein_div_kernel(unsigned long long* counts) {
 	atomicAdd(counts + 5, checked);
 }
 
+__global__ void markstein_wide_div_kernel(unsigned long long* counts) {
+	unsigned long long bad = 0;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (1u << 28); i += gridDim.x * blockDim.x) {
+		uint32_t h = i * 2654435761u + 12345u;
+		h ^= h >> 15;
+		h *= 2246822519u;
+		h ^= h >> 13;
+		uint32_t g = h * 3266489917u + i;
+		g ^= g >> 16;
+		// Exponents 67..187 (2^-60 .. 2^60), random significands and signs.
+		const float a = __uint_as_float(((h >> 31) << 31) | ((67u + (h >> 8) % 121u) << 23) | (g >> 9));
+		const float b = __uint_as_float((((g >> 30) & 1u) << 31) | ((67u + (g >> 1) % 121u) << 23) | (h & 0x7FFFFFu));
+		bad += risltc::div_markstein(a, b, risltc::rcp_markstein(b)) != __fdiv_rn(a, b);
+	}
+	if (bad) atomicAdd(counts + 6, bad);
+}
+
 }  // namespace
 
 extern "C" int risltc_test_markstein(unsigned long long* counts) {
 	unsigned long long* d = nullptr;
-	cudaError_t e = cudaMalloc(&d, 6 * sizeof(unsigned long long));
-	if (e == cudaSuccess) e = cudaMemset(d, 0, 6 * sizeof(unsigned long long));
+	cudaError_t e = cudaMalloc(&d, 7 * sizeof(unsigned long long));
+	if (e == cudaSuccess) e = cudaMemset(d, 0, 7 * sizeof(unsigned long long));
 	if (e == cudaSuccess) {
 		markstein_unary_kernel<<<152 * 16, 256>>>(d);
 		markstein_div_kernel<<<152 * 16, 256>>>(d);
+		markstein_wide_div_kernel<<<152 * 16, 256>>>(d);
 		e = cudaGetLastError();
 	}
 	if (e == cudaSuccess) e = cudaDeviceSynchronize();
-	if (e == cudaSuccess) e = cudaMemcpy(counts, d, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess) e = cudaMemcpy(counts, d, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
 	cudaFree(d);
 	return (int) e;
 }

@@ -7,7 +7,8 @@ receive: every positive normal float for the square root and the reciprocal
 square root, every float in [2^-126, 2^126) for the reciprocal, every divisor
 in [2, 16) for the edge integral's division (with eight numerators each in
 [0.5, 2); Markstein's theorem makes the quotient correctly rounded for every
-numerator once the reciprocal is).  Exact numerics uses them only where this
+numerator once the reciprocal is), and 2^28 random quotients with operands
+of magnitude 2^-60 to 2^60 for the reservoir replay's divisions.  Exact numerics uses them only where this
 test shows them bit-identical; everything else keeps the intrinsics."""
 import ctypes
 import os
@@ -37,8 +38,8 @@ def test_check_compiles_for_sm103a(tmp_path):
 @pytest.mark.gpu
 def test_markstein_sequences_equal_the_intrinsics_on_every_input(gpu, tmp_path):
     lib = ctypes.CDLL(compile_check(str(tmp_path)))
-    counts = np.zeros(6, np.uint64)
+    counts = np.zeros(7, np.uint64)
     assert lib.risltc_test_markstein(ctypes.c_void_p(counts.ctypes.data)) == 0
-    print("sqrt %d, rcp %d, rsqrt %d, rcp[2,16) %d, div %d of %d" % tuple(int(c) for c in counts))
+    print("sqrt %d, rcp %d, rsqrt %d, rcp[2,16) %d, div %d of %d, wide div %d" % tuple(int(c) for c in counts))
     assert counts[5] == 8 * (0x41800000 - 0x40000000)
-    assert list(counts[:5]) == [0, 0, 0, 0, 0]
+    assert list(counts[:5]) == [0, 0, 0, 0, 0] and counts[6] == 0
