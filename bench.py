@@ -531,6 +531,10 @@ def roofline_of(kernels, fp32_peak, flops_per_sample, samples_per_step, ms_per_s
             "frac": d["frac"], "traffic": traffic, "traffic_source": source, "kernel": dominant,
             "flops_per_sample": d["flops_per_sample"],
             "whole_step_frac": flops_per_sample * samples_per_step / (ms_per_step / 1e3) / 1e12 / fp32_peak,
+            # Exact numerics never contracts a multiply and an add (its
+            # results equal an oracle without fused operations), so one FP32
+            # instruction performs at most one of the counted operations.
+            "unfused_peak": fp32_peak / 2, "frac_of_unfused_peak": 2 * d["frac"],
             "peak_source": "derived: 2 x 128 FP32 lanes x %d SMs x %.0f MHz (max SM clock of MEASURED_PEAKS.json); "
                            "no measured FP32 peak exists" % (sms, sm_max)}
 

@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(128, RISLTC_TRACE_MIN_BLOCKS) shadow_trace_ker
 			continue;
 		}
 		if (busy) {
-			const int st = trace_queue_step<P>(s, r, stack, error);
+			const int st = trace_step<P>(s, r, stack, error);
 			if (st != kTraceContinue) {
 				hits[slot] = st == kTraceHit ? 1 : 0;
 				busy = false;

@@ -48,7 +48,6 @@ struct TraceRay {
 	float t_min, t_max;
 	int32_t node;     // next reference to visit (kNoNode: pop the stack)
 	uint32_t leaf_first, leaf_left;  // triangles of the current leaf still to test
-	int32_t pending;  // a leaf reference waiting for the current leaf (dual steps), or kNoNode
 	int sp;
 	uint32_t visits;
 	bool minmax;      // no slab product can be NaN: the min/max form applies
@@ -121,7 +120,6 @@ template <class P> RL_DEV int trace_begin(const SceneView& s, TraceRay& r, f3 o,
 	r.visits = 0;
 	r.leaf_left = 0;
 	r.leaf_first = 0;
-	r.pending = INT32_MIN;
 	// Boxes are finite (the scene rejects non-finite triangles); with a
 	// finite origin and finite non-zero inv no slab product is NaN, and with
 	// t_min and t_max not NaN neither is an interval end.
@@ -203,55 +201,6 @@ template <class P> RL_DEV int trace_step(const SceneView& s, TraceRay& r, int32_
 	const int work = trace_next(r, stack);
 	if (work == kWorkDone) return kTraceMiss;
 	return work == kWorkTriangle ? trace_triangle<P>(s, r) : trace_node(s, r, stack, error);
-}
-
-// Dual step (RISLTC_TRACE_DUAL): one triangle of the open leaf and one inner
-// node in the same step, so a ray with a leaf open keeps walking the tree;
-// a leaf reached while one is open waits in the pending slot, and the walk
-// pauses only while both are taken.  Every reference is still visited
-// exactly when its path's boxes are hit, so the answers are unchanged.
-RL_DEV void open_leaf(TraceRay& r, int32_t ref) {
-	const uint32_t code = (uint32_t) (-(ref + 1));
-	r.leaf_first = code >> 3;
-	r.leaf_left = code & 7u;
-}
-template <class P> RL_DEV int trace_step_dual(const SceneView& s, TraceRay& r, int32_t* stack, uint32_t* error) {
-	if (++r.visits > kTraversalLimit) {
-		atomicOr(error, kErrorTraversalLimit);
-		return kTraceMiss;
-	}
-	if (r.leaf_left == 0 && r.pending != kNoNode) {
-		open_leaf(r, r.pending);
-		r.pending = kNoNode;
-	}
-	if (r.node == kNoNode && r.sp != 0 && (r.leaf_left == 0 || r.pending == kNoNode)) r.node = stack[--r.sp];
-	if (r.node != kNoNode) {
-		if (r.node < 0) {
-			if (r.leaf_left == 0) {
-				open_leaf(r, r.node);
-				r.node = kNoNode;
-			} else if (r.pending == kNoNode) {
-				r.pending = r.node;
-				r.node = kNoNode;
-			}
-		} else if (trace_node(s, r, stack, error) != kTraceContinue) {
-			return kTraceMiss;
-		}
-	}
-	if (r.leaf_left != 0 && trace_triangle<P>(s, r) == kTraceHit) return kTraceHit;
-	if (r.leaf_left == 0 && r.pending == kNoNode && r.node == kNoNode && r.sp == 0) return kTraceMiss;
-	return kTraceContinue;
-}
-#ifndef RISLTC_TRACE_DUAL
-#define RISLTC_TRACE_DUAL 0
-#endif
-// The step of the wavefront trace kernels.
-template <class P> RL_DEV int trace_queue_step(const SceneView& s, TraceRay& r, int32_t* stack, uint32_t* error) {
-#if RISLTC_TRACE_DUAL
-	return trace_step_dual<P>(s, r, stack, error);
-#else
-	return trace_step<P>(s, r, stack, error);
-#endif
 }
 
 // Any-hit query; true if occluded.
