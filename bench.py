@@ -440,6 +440,7 @@ def measure_throughput(a, rl, torch, ctx, fr, rank, world, local_rank, dist, ste
     rl.shade(ctx, fr.scene, fr.g, hs.width, hs.height, so, noise_seed=seed, frames=a.spp, out_rgb=out, primitive=fr.prim)
     torch.cuda.synchronize()
     other_ms = 0.0
+    ctx.profile(True)
     for _ in range(steps):
         if flush is not None:
             flush.fill_(1)
@@ -450,8 +451,11 @@ def measure_throughput(a, rl, torch, ctx, fr, rank, world, local_rank, dist, ste
         o1.record(stream)
         torch.cuda.synchronize()
         other_ms += o0.elapsed_time(o1)
+    po = ctx.profile(False)
+    pcalls = max(po["calls"], 1)
     res["other_numerics"] = {"numerics": other, "value": samples_per_step * steps / (other_ms / 1000.0) / 1e9,
-                             "unit": "Gsamples/s"}
+                             "unit": "Gsamples/s",
+                             "ms_per_launch": {k: v / pcalls for k, v in po.items() if k != "calls"}}
     # End to end through the host entry point: pinned G-buffer in, RGB out.
     res["e2e"] = None
     if not a.no_e2e:
@@ -744,6 +748,13 @@ def run_ours(a, rank, world, local_rank):
     if info:
         roofline = roofline_of(kernels, fp32_peak, info["flops_per_sample"], thr["samples_per_step"],
                                thr["ms_per_step"], sms, sm_max, traffic_key(a))
+        other = thr["other_numerics"]
+        oms = other.get("ms_per_launch", {}).get("candidates", 0.0)
+        if roofline and oms > 0 and roofline["kernel"] == "ris_candidates_binned_kernel":
+            # The same kernel and op count in the other numerics mode.
+            ach = roofline["flops_per_sample"] * thr["samples_per_step"] / (oms / 1e3) / 1e12
+            roofline["other_numerics"] = {"numerics": other["numerics"], "ms_per_launch": oms, "achieved": ach,
+                                          "frac": ach / fp32_peak}
     cpu = None
     if info:
         cpu = {"value": info["samples"] / info["seconds"] / 1e9, "unit": "Gsamples/s", "cores": info["threads"],

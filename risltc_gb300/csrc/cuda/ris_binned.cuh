@@ -54,22 +54,7 @@ constexpr int kFrameWords = 45;              // 44 used; odd stride avoids bank 
 constexpr int kBinnedWarps = 4;              // warps per block
 constexpr int kBins = kMaxLightVertices - 2; // vertex counts 3..8
 
-// Light records of the items a warp evaluates, staged in shared memory: each
-// lane copies its item's record (kLightWords / 4 float4) with cp.async before
-// the evaluation round, so the round waits once for all of them instead of
-// once per vertex pass.  Slots are kStageWords float4 apart (176 bytes: the
-// eight lanes of a quarter-warp 16-byte load hit distinct banks).
-#ifndef RISLTC_STAGE_RECORDS
-#define RISLTC_STAGE_RECORDS 0
-#endif
-constexpr bool kStageRecords = RISLTC_STAGE_RECORDS != 0;
-constexpr int kStageWords = kLightWords / 4 + 1;
-template <bool kStage> struct RecordStage {
-	float4 rec[32][kStageWords];
-};
-template <> struct RecordStage<false> {};
-
-template <int kSuper, int kPixels, int kChunk> struct WarpTile : RecordStage<kStageRecords> {
+template <int kSuper, int kPixels, int kChunk> struct WarpTile {
 	static constexpr int kItems = kPixels * kChunk;  // items per warp per chunk
 	static constexpr int kDeferred = kItems + 32;     // deferred items pending at most
 	static_assert(kItems < 1024, "10-bit bin counters");
@@ -107,27 +92,6 @@ RL_DEV void store_frame(float* f, const CandidateFrame& cf) {
 	}
 }
 
-// Word j (a float4) of a light record: through the read-only data cache from
-// global memory, or a plain load from the warp's staging slot in shared
-// memory.
-template <bool kShared> RL_DEV float4 record_word(const float4* record, uint32_t j) {
-	if constexpr (kShared)
-		return record[j];
-	else
-		return __ldg(record + j);
-}
-
-// Copies a light record (kLightWords / 4 float4, 16-byte aligned at both
-// ends) into a staging slot with asynchronous 16-byte copies that bypass L1.
-RL_DEV void stage_record(float4* slot, const float4* record) {
-	const uint32_t dst = (uint32_t) __cvta_generic_to_shared(slot);
-#pragma unroll
-	for (int w = 0; w != kLightWords / 4; ++w)
-		asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst + 16u * w), "l"(record + w) : "memory");
-}
-// Waits for this thread's outstanding cp.async copies.
-RL_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 // A light vertex (slot j of the record) in local space: mat4x3 * vec4(v, 1)
 // with y negated when negate_y is set (the side flip).
 RL_DEV f3 local_vertex(const mat43& t, const float4* record, uint32_t j, bool negate_y) {
@@ -160,14 +124,9 @@ __device__ __noinline__ float clipped_integral(mat43 t, const float4* record, ui
 // The code stays small and the vertex count of a sorted group is uniform
 // across the warp.  With allow_clip false, returns false as soon as a space
 // clips the polygon partially; the caller defers the item.
-#ifndef RISLTC_SCALAR_PIPELINE
-#define RISLTC_SCALAR_PIPELINE 0
-#endif
-// kShared: the record is a copy in shared memory; such calls never clip
-// (allow_clip must be false), since clipped_integral reads the global record.
-template <class P, bool kShared>
+template <class P>
 RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
-	const float4 head = record_word<kShared>(record, 0), pl = record_word<kShared>(record, 1);
+	const float4 head = __ldg(record), pl = __ldg(record + 1);
 	const uint32_t n = __float_as_uint(head.w);
 	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
 	const bool flip = plane_dot(mk3(f[0], f[1], f[2]), plane) < 0.0f;
@@ -180,49 +139,25 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 #pragma unroll
 		for (int c = 0; c != 4; ++c) t.c[c] = mk3(m[3 * c], m[3 * c + 1], m[3 * c + 2]);
 		const bool negate_y = s == 0 && flip;
-		float4 q = record_word<kShared>(record, 2);
+		float4 q = __ldg(record + 2);
 		f3 v = mul_point(t, mk3(q.x, q.y, q.z));
 		v.y = negate_y ? -v.y : v.y;
-		q = record_word<kShared>(record, 3);
+		q = __ldg(record + 3);
 		uint32_t above = v.z > 0.0f ? 1u : 0u;
 		const f3 first = normalize<P>(v);
-		float r = 0.0f;
-#if RISLTC_SCALAR_PIPELINE
-		// Vertex j + 1 is transformed and normalised while edge (j - 1, j) is
-		// integrated (two independent dependency chains in one basic block);
-		// the last two edges follow the loop.  n >= 3, so vertices 0-2 exist.
-		v = mul_point(t, mk3(q.x, q.y, q.z));
-		v.y = negate_y ? -v.y : v.y;
-		q = record_word<kShared>(record, 4);
-		above += v.z > 0.0f ? 1u : 0u;
-		f3 prev = first, cur = normalize<P>(v);
-#pragma unroll 1
-		for (uint32_t j = 1; j != n - 1; ++j) {
-			v = mul_point(t, mk3(q.x, q.y, q.z));
-			v.y = negate_y ? -v.y : v.y;
-			q = record_word<kShared>(record, 2 + min(j + 2, (uint32_t) kMaxLightVertices - 1));
-			above += v.z > 0.0f ? 1u : 0u;
-			const f3 next = normalize<P>(v);
-			r += integrate_edge<P>(prev, cur);
-			prev = cur;
-			cur = next;
-		}
-		r += integrate_edge<P>(prev, cur);
-		r += integrate_edge<P>(cur, first);
-#else
 		f3 prev = first;
+		float r = 0.0f;
 #pragma unroll 1
 		for (uint32_t j = 1; j != n; ++j) {
 			v = mul_point(t, mk3(q.x, q.y, q.z));
 			v.y = negate_y ? -v.y : v.y;
-			q = record_word<kShared>(record, 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
+			q = __ldg(record + 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
 			above += v.z > 0.0f ? 1u : 0u;
 			const f3 cur = normalize<P>(v);
 			r += integrate_edge<P>(prev, cur);
 			prev = cur;
 		}
 		r += integrate_edge<P>(prev, first);
-#endif
 		bool a = false;
 		if (above == n) {
 			r = fabsf(r);
@@ -230,7 +165,7 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 			r = 0.0f;
 			a = true;
 		} else {
-			if (kShared || !allow_clip) return false;
+			if (!allow_clip) return false;
 			r = clipped_integral<P>(t, record, n, negate_y);
 			a = r < 0.0f;
 			r = a ? 0.0f : r;
@@ -370,9 +305,9 @@ template <class P> RL_DEV float2 integrate_edge2(const f3x2& v1, const f3x2& v2)
 	return pmul<P>(cz, ts);
 }
 
-template <class P, bool kShared>
+template <class P>
 RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool allow_clip, float& p_hat) {
-	const float4 head = record_word<kShared>(record, 0), pl = record_word<kShared>(record, 1);
+	const float4 head = __ldg(record), pl = __ldg(record + 1);
 	const uint32_t n = __float_as_uint(head.w);
 	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
 	const bool flip = plane_dot(mk3(f[0], f[1], f[2]), plane) < 0.0f;
@@ -391,8 +326,8 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 	// it integrates edge (j - 1, j), so the two dependency chains overlap.
 	// The edges are added in calculate_ltc's order: (0, 1), ..., (n - 2,
 	// n - 1), then (n - 1, 0).
-	const float4 q0 = record_word<kShared>(record, 2), q1 = record_word<kShared>(record, 3);
-	float4 q = record_word<kShared>(record, 4);
+	const float4 q0 = __ldg(record + 2), q1 = __ldg(record + 3);
+	float4 q = __ldg(record + 4);
 	f3x2 v = mul_point2<P>(t, q0);
 	if (flip) v.y.x = -v.y.x;
 	uint32_t above_s = v.z.x > 0.0f ? 1u : 0u, above_c = v.z.y > 0.0f ? 1u : 0u;
@@ -409,7 +344,7 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 		if (j + 1 != n) {
 			v = mul_point2<P>(t, q);
 			if (flip) v.y.x = -v.y.x;
-			q = record_word<kShared>(record, 2 + min(j + 2, (uint32_t) kMaxLightVertices - 1));
+			q = __ldg(record + 2 + min(j + 2, (uint32_t) kMaxLightVertices - 1));
 			above_s += v.z.x > 0.0f ? 1u : 0u;
 			above_c += v.z.y > 0.0f ? 1u : 0u;
 			next = normalize2<P>(v);
@@ -420,7 +355,7 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 	}
 	r = padd<P>(r, integrate_edge2<P>(prev, first));
 	const bool partial_s = above_s != n && above_s != 0, partial_c = above_c != n && above_c != 0;
-	if ((partial_s || partial_c) && (kShared || !allow_clip)) return false;
+	if ((partial_s || partial_c) && !allow_clip) return false;
 	float integral[2];
 	bool away[2];
 	const uint32_t above[2] = {above_s, above_c};
@@ -462,23 +397,17 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 // where the paired structure with one scalar operation per lane measured
 // slower (29.4 against 24.7 ms per 4-frame launch of the candidate kernel).
 // RISLTC_CANDIDATE_PAIRS=1 selects the paired form for exact numerics too.
-template <class P, bool kShared = false> struct CandidateEval {
-	static RL_DEV bool run(const float* f, const float4* record, bool allow_clip, float& p_hat) {
-#if RISLTC_CANDIDATE_PAIRS
-		return binned_candidate_pair<P, kShared>(f, record, allow_clip, p_hat);
-#else
-		return binned_candidate<P, kShared>(f, record, allow_clip, p_hat);
-#endif
-	}
-};
-template <bool kShared> struct CandidateEval<FastNumerics, kShared> {
-	static RL_DEV bool run(const float* f, const float4* record, bool allow_clip, float& p_hat) {
-		return binned_candidate_pair<FastNumerics, kShared>(f, record, allow_clip, p_hat);
-	}
-};
-template <class P, bool kShared = false>
+template <class P>
 RL_DEV bool evaluate_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
-	return CandidateEval<P, kShared>::run(f, record, allow_clip, p_hat);
+#if RISLTC_CANDIDATE_PAIRS
+	return binned_candidate_pair<P>(f, record, allow_clip, p_hat);
+#else
+	return binned_candidate<P>(f, record, allow_clip, p_hat);
+#endif
+}
+template <>
+RL_DEV bool evaluate_candidate<FastNumerics>(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+	return binned_candidate_pair<FastNumerics>(f, record, allow_clip, p_hat);
 }
 
 // One warp tile t (pixels t * kPixels .. + kPixels - 1) of one frame set:
@@ -592,22 +521,12 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 					//    pending.
 					for (uint32_t base = 0; base < item_count; base += 32) {
 						const uint32_t it = base + lane;
-						if constexpr (kStageRecords) {
-							// Each lane stages and then reads only its own slot.
-							if (it < item_count) stage_record(tile.rec[lane], light_record(pr.scene, (int32_t) (tile.item[it] >> 10)));
-							cp_async_wait_all();
-						}
 						if (it < item_count) {
 							const uint32_t item = tile.item[it];
 							const uint32_t slot = item & 1023u;
 							const int32_t l = (int32_t) (item >> 10);
 							float ph;
-							bool done;
-							if constexpr (kStageRecords)
-								done = evaluate_candidate<P, true>(tile.frame[slot / kSuper], tile.rec[lane], false, ph);
-							else
-								done = evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph);
-							if (done) {
+							if (evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph)) {
 								phat[slot] = ph;
 							} else {
 								const uint32_t d = atomicAdd(&tile.deferred_count, 1u);
