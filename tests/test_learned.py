@@ -47,8 +47,12 @@ def test_model_logits_match_numpy(gpu, k):
     want = reference_logits(params, k, encode(sc["gbuffer"], center, half))
     err = np.abs(got - want)
     scale = np.abs(want).max()
-    assert np.quantile(err, 0.999) <= 0.02 * scale
-    assert err.max() <= 0.08 * scale
+    # The restatement rounds to BF16 where the kernel does; they differ only
+    # where an FP32 sum in another order lands on the other side of a BF16
+    # rounding boundary (one BF16 step is 2^-8 relative; measured largest
+    # difference 0.23% of the largest logit, median 0).
+    assert np.quantile(err, 0.999) <= 0.005 * scale
+    assert err.max() <= 0.01 * scale
     print("logits: scale %.3f, median error %.2e, max error %.2e" % (scale, np.median(err), err.max()))
 
 
@@ -156,7 +160,8 @@ def test_model_logits_unaligned_frame(gpu):
     ctx.close()
     want = reference_logits(params, 64, encode(g_host, center, half))
     err = np.abs(got - want)
-    assert err.max() <= 0.08 * np.abs(want).max()
+    print("ragged logits: scale %.3f, max error %.2e" % (np.abs(want).max(), err.max()))
+    assert err.max() <= 0.01 * np.abs(want).max()
 
 
 @pytest.mark.gpu
