@@ -85,11 +85,12 @@ cudaError_t launch_candidates_batch(const RisBatch& b, cudaStream_t stream, int 
 }
 
 template <class P>
-__global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_batch_kernel(const __grid_constant__ RisBatch b) {
+__global__ void __launch_bounds__(kSampleThreads, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_batch_kernel(const __grid_constant__ RisBatch b) {
+	__shared__ PsaPolygon poly[kSampleThreads];
 	const uint32_t total = b.pixel_begin[b.count];
 	for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < total; u += gridDim.x * blockDim.x) {
 		const uint32_t k = batch_item(b.pixel_begin, b.count, u);
-		sample_pixel<P>(b.item[k], u - b.pixel_begin[k]);
+		sample_pixel<P>(b.item[k], u - b.pixel_begin[k], poly[threadIdx.x]);
 	}
 }
 

@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(128, RISLTC_CANDIDATE_MIN_BLOCKS) ris_candidat
 	}
 }
 
-template <class P> __global__ void __launch_bounds__(128) ris_shade_kernel(RisParams pr) {
+template <class P> __global__ void __launch_bounds__(kShadeThreads) ris_shade_kernel(RisParams pr) {
+	__shared__ PsaPolygon polys[2][kShadeThreads];
 	const uint32_t np = pr.width * pr.height;
 	ShadeParams sp;  // the fields psa_mis_shade and polygon_visibility read
 	sp.scene = pr.scene;
@@ -278,7 +279,7 @@ template <class P> __global__ void __launch_bounds__(128) ris_shade_kernel(RisPa
 				Light l;
 				load_light(pr.scene, r.light_index, l);
 				uint32_t seed = r.seed;
-				f3 color = psa_mis_shade<P>(sp, sd, ltc, l, seed, true, true);
+				f3 color = psa_mis_shade<P>(sp, sd, ltc, l, seed, true, true, polys[0][threadIdx.x], polys[1][threadIdx.x]);
 				float W = P::div(r.w_sum, (float) pr.candidate_count * r.p_hat);
 				if (r.p_hat == 0.0f) W = 0.0f;
 				f3 cw = scale(color, W);

@@ -65,10 +65,12 @@ RL_DEV void store_contributions(SampleRecord* dst, int j, f3 c0, f3 c1) {
 // visibility test.  Writes both techniques' contributions into *dst (zero
 // where a technique has none) and each traced technique's shadow ray into
 // staged[j] as soon as they are known, and returns the techniques' modes.
-// l is the light whose device record is `record`.
+// l is the light whose device record is `record`; poly is the thread's
+// polygon buffer.
 template <class P>
 RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l,
-                             const float4* record, uint32_t& seed, SampleRecord* dst, ShadowRay* staged) {
+                             const float4* record, uint32_t& seed, SampleRecord* dst, ShadowRay* staged,
+                             PsaPolygon& poly) {
 	const bool fa = pr.fast_atan != 0;
 	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
 	side_flip(ltc, sd, l);
@@ -79,7 +81,6 @@ RL_DEV uint32_t psa_mis_emit(const ShadeParams& pr, const ShadingData& sd, Ltc l
 	// specular), and after sampling only the projected solid angles are
 	// needed, so the values equal those of psa_prepare_both followed by both
 	// samples.
-	PsaPolygon poly;
 	float psa[2] = {0.0f, 0.0f};
 	int technique_count = 1;
 	f3 dir_d = mk3(0.0f, 0.0f, 1.0f), dir_s = mk3(0.0f, 0.0f, 1.0f);
@@ -173,9 +174,16 @@ RL_DEV void store_sample(SampleRecord* dst, const f3 (&c)[2][2], float W, uint32
 #ifndef RISLTC_SAMPLE_MIN_BLOCKS
 #define RISLTC_SAMPLE_MIN_BLOCKS 4
 #endif
+// Threads per block of the sample kernels.  Each thread's PSA polygon buffer
+// (196 bytes, indexed by the sorting network and the sector search) is a
+// slot of a shared-memory array: slots are 49 words apart, so the lanes'
+// words of one index fall in 32 distinct banks.  In local memory the 16
+// resident warps' buffers (about 240 KB per SM) did not stay in L1 (sample
+// kernel 5.71 ms per 4-frame 1080p launch, 4.14 ms with the shared slots).
+constexpr int kSampleThreads = 128;
 // The sample phase of pixel i (all frames of the call); i may be past the
 // frame (the thread then does nothing).
-template <class P> RL_DEV void sample_pixel(const RisParams& pr, uint32_t i) {
+template <class P> RL_DEV void sample_pixel(const RisParams& pr, uint32_t i, PsaPolygon& poly) {
 	const uint32_t np = pr.width * pr.height;
 	ShadeParams sp;  // the fields psa_prepare_both and psa_mis_emit read
 	sp.scene = pr.scene;
@@ -216,7 +224,7 @@ template <class P> RL_DEV void sample_pixel(const RisParams& pr, uint32_t i) {
 					uint32_t seed = r.seed;
 					// Contributions and staged rays go to memory inside.
 					modes = psa_mis_emit<P>(sp, sd, ltc, l, light_record(pr.scene, r.light_index), seed,
-					                        pr.samples + pf, pr.staged + 2 * pf);
+					                        pr.samples + pf, pr.staged + 2 * pf, poly);
 					float W = P::div(r.w_sum, (float) pr.candidate_count * r.p_hat);
 					if (r.p_hat == 0.0f) W = 0.0f;
 					*reinterpret_cast<float2*>(reinterpret_cast<float*>(pr.samples + pf) + 12) =
@@ -234,10 +242,11 @@ template <class P> RL_DEV void sample_pixel(const RisParams& pr, uint32_t i) {
 }
 
 template <class P>
-__global__ void __launch_bounds__(128, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_kernel(const __grid_constant__ RisParams pr) {
+__global__ void __launch_bounds__(kSampleThreads, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_kernel(const __grid_constant__ RisParams pr) {
+	__shared__ PsaPolygon poly[kSampleThreads];
 	const uint32_t np = pr.width * pr.height;
 	for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x)
-		sample_pixel<P>(pr, base + threadIdx.x);
+		sample_pixel<P>(pr, base + threadIdx.x, poly[threadIdx.x]);
 }
 
 // Exclusive prefix sum of the per-light ray counts, in place (each becomes

@@ -8,9 +8,9 @@ namespace risltc {
 cudaError_t launch_shade(const ShadeParams& p, cudaStream_t stream, int grid, cudaEvent_t* events, bool fast) {
 	if (events) cudaEventRecord(events[0], stream);
 	if (fast)
-		shade_kernel<FastNumerics, ExactNumerics><<<grid, 128, 0, stream>>>(p);
+		shade_kernel<FastNumerics, ExactNumerics><<<grid, kShadeThreads, 0, stream>>>(p);
 	else
-		shade_kernel<ExactNumerics, ExactNumerics><<<grid, 128, 0, stream>>>(p);
+		shade_kernel<ExactNumerics, ExactNumerics><<<grid, kShadeThreads, 0, stream>>>(p);
 	cudaError_t e = cudaGetLastError();
 	if (events)
 		for (int k = 1; k != RISLTC_PROFILE_PHASES + 1; ++k) cudaEventRecord(events[k], stream);
@@ -26,7 +26,7 @@ cudaError_t launch_candidates_exact(const RisParams& p, cudaStream_t stream, int
 	return launch_candidates_tile_exact(p, stream, grid_cap, tile);
 }
 cudaError_t launch_ris_shade(const RisParams& p, cudaStream_t stream, int grid) {
-	ris_shade_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	ris_shade_kernel<ExactNumerics><<<grid, kShadeThreads, 0, stream>>>(p);
 	return cudaGetLastError();
 }
 cudaError_t launch_proposal(const ProposalParams& p, cudaStream_t stream, int grid) {
@@ -34,7 +34,7 @@ cudaError_t launch_proposal(const ProposalParams& p, cudaStream_t stream, int gr
 	return cudaGetLastError();
 }
 cudaError_t launch_ris_sample(const RisParams& p, cudaStream_t stream, int grid) {
-	ris_sample_kernel<ExactNumerics><<<grid, 128, 0, stream>>>(p);
+	ris_sample_kernel<ExactNumerics><<<grid, kSampleThreads, 0, stream>>>(p);
 	return cudaGetLastError();
 }
 cudaError_t launch_shadow_sort(const RisParams& p, cudaStream_t stream, int grid) {
@@ -57,7 +57,7 @@ cudaError_t launch_candidates_batch_exact(const RisBatch& b, cudaStream_t stream
 	return launch_candidates_batch_tile_exact(b, stream, grid_cap, tile);
 }
 cudaError_t launch_batch_estimator(const RisBatch& b, cudaStream_t stream, int pixel_grid, int pf_grid, int ray_grid) {
-	ris_sample_batch_kernel<ExactNumerics><<<pixel_grid, 128, 0, stream>>>(b);
+	ris_sample_batch_kernel<ExactNumerics><<<pixel_grid, kSampleThreads, 0, stream>>>(b);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
 	light_bucket_scan_batch_kernel<<<b.count, 1024, 0, stream>>>(b);

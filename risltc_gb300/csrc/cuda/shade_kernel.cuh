@@ -305,13 +305,19 @@ RL_DEV bool psa_prepare_both(const ShadeParams& pr, const ShadingData& sd, Ltc& 
 	return pd.psa != 0.0f;
 }
 
+// Threads per block of the kernels that shade with psa_mis_shade.  Each
+// thread's two PSA polygon buffers (196 bytes each, dynamically indexed)
+// are slots of shared-memory arrays, 49 words apart, so the lanes' words of
+// one index fall in distinct banks; in local memory the resident warps'
+// buffers did not stay in L1.
+constexpr int kShadeThreads = 128;
+// pd and ps are the thread's two polygon buffers.
 template <class P>
 RL_DEV f3 psa_mis_shade(const ShadeParams& pr, const ShadingData& sd, Ltc ltc, const Light& l, uint32_t& seed,
-                        bool peters, bool visibility_in) {
+                        bool peters, bool visibility_in, PsaPolygon& pd, PsaPolygon& ps) {
 	const bool fa = pr.fast_atan != 0;
 	const bool biased = pr.technique == sample_polygon_projected_solid_angle_biased;
 	f3 result = splat(0.0f);
-	PsaPolygon pd, ps;
 	if (!psa_prepare_both<P>(pr, sd, ltc, l, pd, ps)) return result;
 	float specular_weight = ltc.albedo * ps.psa;
 	f3 diffuse_weight = scale(max3(sd.diffuse_albedo, splat(0.01f)), pd.psa);
@@ -419,7 +425,7 @@ RL_DEV f3 area_turk_shade(const ShadeParams& pr, const ShadingData& sd, const Li
 
 template <class C, class P>
 RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& ltc, uint32_t seed, bool first_frame,
-                      risltc_reservoir_t* res_out) {
+                      risltc_reservoir_t* res_out, PsaPolygon& pd, PsaPolygon& ps) {
 	const int n = pr.scene.light_count;
 	const bool peters = pr.technique == sample_polygon_ltc_cp;
 	const bool area_turk = pr.technique == sample_polygon_area_turk;
@@ -440,7 +446,7 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 			load_light(pr.scene, idx, l);
 			bool visibility = true;
 			const f3 shade = area_turk ? area_turk_shade<P>(pr, sd, l, light_sample, false, visibility, seed)
-			                           : psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true);
+			                           : psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true, pd, ps);
 			f3 r = scale(shade, (float) n);
 			float ls = (float) pr.light_samples;
 			r = mk3(P::div(r.x, ls), P::div(r.y, ls), P::div(r.z, ls));
@@ -466,7 +472,7 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 					bool dummy_visibility = false;
 					color = area_turk_shade<C>(pr, sd, l, light_sample, false, dummy_visibility, seed);
 				} else {
-					color = psa_mis_shade<C>(pr, sd, ltc, l, seed, false, false);
+					color = psa_mis_shade<C>(pr, sd, ltc, l, seed, false, false, pd, ps);
 				}
 				float p_hat = C::sqrt(dot(color, color));
 				float w = C::div(p_hat, p);
@@ -489,7 +495,7 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 				load_light(pr.scene, res_index, l);
 				bool visibility = true;
 				const f3 color = area_turk ? area_turk_shade<P>(pr, sd, l, res_light_sample, true, visibility, seed)
-				                           : psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true);
+				                           : psa_mis_shade<P>(pr, sd, ltc, l, seed, peters, true, pd, ps);
 				float W = P::div(w_sum, (float) m * sample_value);
 				// The area technique has no p_hat == 0 guard but multiplies by
 				// the traced visibility (shading_pass.frag.glsl:749-756).
@@ -508,7 +514,8 @@ RL_DEV f3 shade_pixel(const ShadeParams& pr, const ShadingData& sd, const Ltc& l
 	return final_color;
 }
 
-template <class C, class P> __global__ void __launch_bounds__(128) shade_kernel(ShadeParams pr) {
+template <class C, class P> __global__ void __launch_bounds__(kShadeThreads) shade_kernel(ShadeParams pr) {
+	__shared__ PsaPolygon polys[2][kShadeThreads];
 	const uint32_t np = pr.width * pr.height;
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
 		const uint32_t x = i % pr.width, y = i / pr.width;
@@ -538,7 +545,7 @@ template <class C, class P> __global__ void __launch_bounds__(128) shade_kernel(
 		for (uint32_t f = 0; f != pr.frame_count; ++f) {
 			uint32_t rn_x = pr.animate ? wang_random_number((pr.noise_seed + f) * 4u) : 0u;
 			uint32_t seed = get_noise_accessor(x, y, pr.width, rn_x);
-			f3 c = shade_pixel<C, P>(pr, sd, ltc, seed, f == 0, res);
+			f3 c = shade_pixel<C, P>(pr, sd, ltc, seed, f == 0, res, polys[0][threadIdx.x], polys[1][threadIdx.x]);
 			sum = add(sum, c);
 			acc[0] += (double) c.x;
 			acc[1] += (double) c.y;
