@@ -298,7 +298,7 @@ template <class P> RL_DEV float2 integrate_edge2(const f3x2& v1, const f3x2& v2)
 	const float2 y = make_float2(fabsf(x.x), fabsf(x.y));
 	const float2 a = padd<P>(pair(0.8543985f), pmul<P>(mad2<P>(pair(0.0145206f), y, pair(0.4965155f)), y));
 	const float2 b = padd<P>(pair(3.4175940f), pmul<P>(padd<P>(pair(4.1616724f), y), y));
-	float2 ts = make_float2(P::div(a.x, b.x), P::div(a.y, b.y));
+	float2 ts = make_float2(P::div_edge(a.x, b.x), P::div_edge(a.y, b.y));
 	if (!(x.x > 0.0f)) ts.x = 0.5f * P::rsqrt(fmax_glsl(1.0f - x.x * x.x, 1e-7f)) - ts.x;
 	if (!(x.y > 0.0f)) ts.y = 0.5f * P::rsqrt(fmax_glsl(1.0f - x.y * x.y, 1e-7f)) - ts.y;
 	const float2 cz = padd<P>(pmul<P>(v1.x, v2.y), pmul<P>(make_float2(-v1.y.x, -v1.y.y), v2.x));
