@@ -51,7 +51,7 @@ RL_DEV uint32_t batch_item(const uint32_t* begin, uint32_t count, uint32_t u) {
 }
 
 template <class P, int kPixels, int kChunk>
-__global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
+__global__ void __launch_bounds__(32 * kBinnedWarps, BinnedMinBlocks<P>::value)
 ris_candidates_batch_kernel(const __grid_constant__ RisBatch b) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	using Tile = WarpTile<BinnedSuper<P>::value, kPixels, kChunk>;
@@ -67,18 +67,14 @@ ris_candidates_batch_kernel(const __grid_constant__ RisBatch b) {
 template <class P, int kPixels, int kChunk>
 cudaError_t launch_candidates_batch(const RisBatch& b, cudaStream_t stream, int grid_cap) {
 	static std::atomic<uint64_t> configured{0};
+	static std::atomic<int> resident[64];
 	int device = 0;
-	cudaError_t e = cudaGetDevice(&device);
+	const cudaError_t e = configure_candidate_kernel(ris_candidates_batch_kernel<P, kPixels, kChunk>,
+	                                                 binned_smem_bytes<P, kPixels, kChunk>(), configured, resident, device);
 	if (e != cudaSuccess) return e;
-	const uint64_t bit = 1ull << (device & 63);
-	if (!(configured.load() & bit)) {
-		e = cudaFuncSetAttribute(ris_candidates_batch_kernel<P, kPixels, kChunk>,
-		                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int) binned_smem_bytes<P, kPixels, kChunk>());
-		if (e != cudaSuccess) return e;
-		configured.fetch_or(bit);
-	}
 	const size_t blocks = ((size_t) b.tile_begin[b.count] + kBinnedWarps - 1) / kBinnedWarps;
-	const int grid = (int) std::max<size_t>(1, std::min<size_t>(blocks, (size_t) grid_cap));
+	const int grid = (int) std::max<size_t>(
+	    1, std::min<size_t>(blocks, (size_t) std::min(grid_cap, resident[device & 63].load())));
 	ris_candidates_batch_kernel<P, kPixels, kChunk>
 	    <<<grid, 32 * kBinnedWarps, binned_smem_bytes<P, kPixels, kChunk>(), stream>>>(b);
 	return cudaGetLastError();

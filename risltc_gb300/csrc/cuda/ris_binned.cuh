@@ -30,8 +30,15 @@
 
 namespace risltc {
 
-#ifndef RISLTC_BINNED_MIN_BLOCKS
-#define RISLTC_BINNED_MIN_BLOCKS 4
+// Blocks per SM the candidate kernel is compiled for (register budget):
+// measured best 5 in exact numerics (96 registers; 19.2 against 19.9 ms per
+// 4-frame 1080p launch with 4) and 4 in fast numerics, whose paired form
+// spills at 96 registers.
+#ifndef RISLTC_BINNED_MIN_BLOCKS_EXACT
+#define RISLTC_BINNED_MIN_BLOCKS_EXACT 5
+#endif
+#ifndef RISLTC_BINNED_MIN_BLOCKS_FAST
+#define RISLTC_BINNED_MIN_BLOCKS_FAST 4
 #endif
 // A warp's p_hat values of one super-chunk, [pixel lane][candidate], live in
 // its slot of RisParams::p_hat_scratch (global memory, L2/L1): keeping them
@@ -49,6 +56,12 @@ template <class P> struct BinnedSuper {
 };
 template <> struct BinnedSuper<FastNumerics> {
 	static constexpr int value = 16;
+};
+template <class P> struct BinnedMinBlocks {
+	static constexpr int value = RISLTC_BINNED_MIN_BLOCKS_EXACT;
+};
+template <> struct BinnedMinBlocks<FastNumerics> {
+	static constexpr int value = RISLTC_BINNED_MIN_BLOCKS_FAST;
 };
 constexpr int kFrameWords = 45;              // 44 used; odd stride avoids bank conflicts
 constexpr int kBinnedWarps = 4;              // warps per block
@@ -124,8 +137,11 @@ __device__ __noinline__ float clipped_integral(mat43 t, const float4* record, ui
 // The code stays small and the vertex count of a sorted group is uniform
 // across the warp.  With allow_clip false, returns false as soon as a space
 // clips the polygon partially; the caller defers the item.
-template <class P>
+template <class P, bool kChecked>
 RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+	// kChecked: normalise with normalize_checked and return false (the item
+	// is deferred) if any square root falls outside its range.
+	bool ok = true;
 	const float4 head = __ldg(record), pl = __ldg(record + 1);
 	const uint32_t n = __float_as_uint(head.w);
 	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
@@ -144,7 +160,7 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 		v.y = negate_y ? -v.y : v.y;
 		q = __ldg(record + 3);
 		uint32_t above = v.z > 0.0f ? 1u : 0u;
-		const f3 first = normalize<P>(v);
+		const f3 first = kChecked ? normalize_checked<P>(v, ok) : normalize<P>(v);
 		f3 prev = first;
 		float r = 0.0f;
 #pragma unroll 1
@@ -153,11 +169,12 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 			v.y = negate_y ? -v.y : v.y;
 			q = __ldg(record + 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
 			above += v.z > 0.0f ? 1u : 0u;
-			const f3 cur = normalize<P>(v);
+			const f3 cur = kChecked ? normalize_checked<P>(v, ok) : normalize<P>(v);
 			r += integrate_edge<P>(prev, cur);
 			prev = cur;
 		}
 		r += integrate_edge<P>(prev, first);
+		if (kChecked && !ok) return false;
 		bool a = false;
 		if (above == n) {
 			r = fabsf(r);
@@ -292,6 +309,15 @@ template <class P> RL_DEV f3x2 normalize2(const f3x2& a) {
 	const float2 s = make_float2(P::rsqrt(d.x), P::rsqrt(d.y));
 	return {pmul<P>(a.x, s), pmul<P>(a.y, s), pmul<P>(a.z, s)};
 }
+// normalize2 with the branch-free square root of normalize_checked (exact
+// numerics; ok cleared outside its range).
+template <class P> RL_DEV f3x2 normalize2_checked(const f3x2& a, bool& ok) { return normalize2<P>(a); }
+template <> RL_DEV f3x2 normalize2_checked<ExactNumerics>(const f3x2& a, bool& ok) {
+	const float2 d = dot2<ExactNumerics>(a, a);
+	ok = ok && tuckerman_range(d.x) && tuckerman_range(d.y);
+	const float2 s = make_float2(rcp_markstein(sqrt_tuckerman(d.x)), rcp_markstein(sqrt_tuckerman(d.y)));
+	return {pmul<ExactNumerics>(a.x, s), pmul<ExactNumerics>(a.y, s), pmul<ExactNumerics>(a.z, s)};
+}
 // integrate_edge on both lanes.
 template <class P> RL_DEV float2 integrate_edge2(const f3x2& v1, const f3x2& v2) {
 	const float2 x = dot2<P>(v1, v2);
@@ -305,8 +331,9 @@ template <class P> RL_DEV float2 integrate_edge2(const f3x2& v1, const f3x2& v2)
 	return pmul<P>(cz, ts);
 }
 
-template <class P>
+template <class P, bool kChecked = false>
 RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+	bool ok = true;
 	const float4 head = __ldg(record), pl = __ldg(record + 1);
 	const uint32_t n = __float_as_uint(head.w);
 	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
@@ -331,12 +358,12 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 	f3x2 v = mul_point2<P>(t, q0);
 	if (flip) v.y.x = -v.y.x;
 	uint32_t above_s = v.z.x > 0.0f ? 1u : 0u, above_c = v.z.y > 0.0f ? 1u : 0u;
-	const f3x2 first = normalize2<P>(v);
+	const f3x2 first = kChecked ? normalize2_checked<P>(v, ok) : normalize2<P>(v);
 	v = mul_point2<P>(t, q1);
 	if (flip) v.y.x = -v.y.x;
 	above_s += v.z.x > 0.0f ? 1u : 0u;
 	above_c += v.z.y > 0.0f ? 1u : 0u;
-	f3x2 prev = first, cur = normalize2<P>(v);
+	f3x2 prev = first, cur = kChecked ? normalize2_checked<P>(v, ok) : normalize2<P>(v);
 	float2 r = pair(0.0f);
 #pragma unroll kPairUnroll
 	for (uint32_t j = 1; j != n; ++j) {
@@ -347,13 +374,14 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 			q = __ldg(record + 2 + min(j + 2, (uint32_t) kMaxLightVertices - 1));
 			above_s += v.z.x > 0.0f ? 1u : 0u;
 			above_c += v.z.y > 0.0f ? 1u : 0u;
-			next = normalize2<P>(v);
+			next = kChecked ? normalize2_checked<P>(v, ok) : normalize2<P>(v);
 		}
 		r = padd<P>(r, integrate_edge2<P>(prev, cur));
 		prev = cur;
 		cur = next;
 	}
 	r = padd<P>(r, integrate_edge2<P>(prev, first));
+	if (kChecked && !ok) return false;
 	const bool partial_s = above_s != n && above_s != 0, partial_c = above_c != n && above_c != 0;
 	if ((partial_s || partial_c) && !allow_clip) return false;
 	float integral[2];
@@ -400,9 +428,13 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 template <class P>
 RL_DEV bool evaluate_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
 #if RISLTC_CANDIDATE_PAIRS
-	return binned_candidate_pair<P>(f, record, allow_clip, p_hat);
+	return allow_clip ? binned_candidate_pair<P, false>(f, record, true, p_hat)
+	                  : binned_candidate_pair<P, true>(f, record, false, p_hat);
 #else
-	return binned_candidate<P>(f, record, allow_clip, p_hat);
+	// The first pass (allow_clip false) takes the branch-free square root;
+	// deferred items are evaluated with the general one.
+	return allow_clip ? binned_candidate<P, false>(f, record, true, p_hat)
+	                  : binned_candidate<P, true>(f, record, false, p_hat);
 #endif
 }
 template <>
@@ -595,7 +627,7 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 }
 
 template <class P, int kPixels, int kChunk>
-__global__ void __launch_bounds__(32 * kBinnedWarps, RISLTC_BINNED_MIN_BLOCKS)
+__global__ void __launch_bounds__(32 * kBinnedWarps, BinnedMinBlocks<P>::value)
 ris_candidates_binned_kernel(const __grid_constant__ RisParams pr) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	using Tile = WarpTile<BinnedSuper<P>::value, kPixels, kChunk>;
@@ -608,6 +640,30 @@ ris_candidates_binned_kernel(const __grid_constant__ RisParams pr) {
 
 template <class P, int kPixels, int kChunk> constexpr size_t binned_smem_bytes() {
 	return sizeof(WarpTile<BinnedSuper<P>::value, kPixels, kChunk>) * kBinnedWarps;
+}
+
+// First launch of a candidate kernel on a device: raises its shared-memory
+// limit (above the 48 KB available without opting in) and stores in
+// resident[device] the blocks that fit on the device at once (resident
+// blocks per SM times the SM count), the kernel's persistent grid: its warps
+// stride over the tiles in one wave, with no partial last wave.  Done once
+// per device, so that later launches, including those captured into a CUDA
+// graph, make no other runtime call.
+template <class Kernel>
+cudaError_t configure_candidate_kernel(Kernel kernel, size_t smem, std::atomic<uint64_t>& configured,
+                                       std::atomic<int>* resident, int& device) {
+	cudaError_t e = cudaGetDevice(&device);
+	if (e != cudaSuccess) return e;
+	const uint64_t bit = 1ull << (device & 63);
+	if (configured.load() & bit) return cudaSuccess;
+	e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+	int sms = 0, per_sm = 0;
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * kBinnedWarps, smem);
+	if (e != cudaSuccess) return e;
+	resident[device & 63].store(std::max(1, sms * per_sm));
+	configured.fetch_or(bit);
+	return cudaSuccess;
 }
 
 // Launches the binned candidate kernel.  Its shared memory exceeds the 48 KB
@@ -627,18 +683,14 @@ cudaError_t launch_candidates_binned(const RisParams& p, cudaStream_t stream, in
 		return cudaGetLastError();
 	}
 	static std::atomic<uint64_t> configured{0};
+	static std::atomic<int> resident[64];
 	int device = 0;
-	cudaError_t e = cudaGetDevice(&device);
+	const cudaError_t e = configure_candidate_kernel(ris_candidates_binned_kernel<P, kPixels, kChunk>,
+	                                                 binned_smem_bytes<P, kPixels, kChunk>(), configured, resident, device);
 	if (e != cudaSuccess) return e;
-	const uint64_t bit = 1ull << (device & 63);
-	if (!(configured.load() & bit)) {
-		e = cudaFuncSetAttribute(ris_candidates_binned_kernel<P, kPixels, kChunk>,
-		                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int) binned_smem_bytes<P, kPixels, kChunk>());
-		if (e != cudaSuccess) return e;
-		configured.fetch_or(bit);
-	}
 	ris_candidates_binned_kernel<P, kPixels, kChunk>
-	    <<<grid, 32 * kBinnedWarps, binned_smem_bytes<P, kPixels, kChunk>(), stream>>>(p);
+	    <<<std::min(grid, resident[device & 63].load()), 32 * kBinnedWarps, binned_smem_bytes<P, kPixels, kChunk>(),
+	       stream>>>(p);
 	return cudaGetLastError();
 }
 

@@ -1,8 +1,9 @@
 // ieee_check.cu - exhaustive check of the Markstein sequences of
-// shade_device.cuh (rcp_markstein, rsqrt_markstein, div_markstein) against
-// CUDA's correctly rounded intrinsics, on this GPU's approximation unit.
+// shade_device.cuh (rcp_markstein, rsqrt_markstein, div_markstein) and of its
+// branch-free square root (sqrt_tuckerman) against CUDA's correctly rounded
+// intrinsics, on this GPU's approximation unit.
 //
-// risltc_test_markstein(counts) fills counts[5]:
+// risltc_test_markstein(counts) fills counts[7]:
 //   0 reciprocals differing from __frcp_rn over every float in [2^-126, 2^126);
 //   1 reciprocal square roots differing from __frcp_rn(__fsqrt_rn(x)) over
 //     every 32-bit pattern x (bitwise; results that are both NaN agree);
@@ -11,7 +12,10 @@
 //     operands lie in [0.85, 1.37] / [3.41, 8.58]);
 //   3 the number of quotients checked;
 //   4 quotients differing over 2^28 pseudo-random pairs with numerators in
-//     [0.85, 1.37] and divisors in [3.41, 8.58].
+//     [0.85, 1.37] and divisors in [3.41, 8.58];
+//   5 square roots differing from __fsqrt_rn over every float in
+//     [2^-76, 2^126];
+//   6 the number of 32-bit patterns tuckerman_range admits.
 // Returns a cudaError_t.
 #include <cuda_runtime.h>
 
@@ -70,20 +74,37 @@ __global__ void markstein_edge_div_kernel(unsigned long long* counts) {
 	if (bad) atomicAdd(counts + 4, bad);
 }
 
+// Every float d in [2^-76, 2^126]: the branch-free square root against
+// __fsqrt_rn (counter 5), and the range test (counter 6 counts the floats it
+// admits; the range holds 0x7e800000 - 0x19800000 + 1 of them).
+__global__ void tuckerman_sqrt_kernel(unsigned long long* counts) {
+	const uint32_t lo = 0x19800000u, hi = 0x7e800000u;
+	unsigned long long bad = 0;
+	for (uint32_t u = lo + blockIdx.x * blockDim.x + threadIdx.x; u <= hi; u += gridDim.x * blockDim.x)
+		bad += !same(risltc::sqrt_tuckerman(__uint_as_float(u)), __fsqrt_rn(__uint_as_float(u)));
+	if (bad) atomicAdd(counts + 5, bad);
+	unsigned long long admitted = 0;
+	for (uint64_t u = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; u < (1ull << 32);
+	     u += (uint64_t) gridDim.x * blockDim.x)
+		admitted += risltc::tuckerman_range(__uint_as_float((uint32_t) u)) ? 1 : 0;
+	atomicAdd(counts + 6, admitted);
+}
+
 }  // namespace
 
 extern "C" int risltc_test_markstein(unsigned long long* counts) {
 	unsigned long long* d = nullptr;
-	cudaError_t e = cudaMalloc(&d, 5 * sizeof(unsigned long long));
-	if (e == cudaSuccess) e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));
+	cudaError_t e = cudaMalloc(&d, 7 * sizeof(unsigned long long));
+	if (e == cudaSuccess) e = cudaMemset(d, 0, 7 * sizeof(unsigned long long));
 	if (e == cudaSuccess) {
 		markstein_unary_kernel<<<152 * 16, 256>>>(d);
 		markstein_div_kernel<<<152 * 16, 256>>>(d);
 		markstein_edge_div_kernel<<<152 * 16, 256>>>(d);
+		tuckerman_sqrt_kernel<<<152 * 16, 256>>>(d);
 		e = cudaGetLastError();
 	}
 	if (e == cudaSuccess) e = cudaDeviceSynchronize();
-	if (e == cudaSuccess) e = cudaMemcpy(counts, d, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess) e = cudaMemcpy(counts, d, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
 	cudaFree(d);
 	return (int) e;
 }
