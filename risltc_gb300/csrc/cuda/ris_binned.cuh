@@ -40,6 +40,7 @@ namespace risltc {
 #ifndef RISLTC_BINNED_MIN_BLOCKS_FAST
 #define RISLTC_BINNED_MIN_BLOCKS_FAST 4
 #endif
+
 // A warp's p_hat values of one super-chunk, [pixel lane][candidate], live in
 // its slot of RisParams::p_hat_scratch (global memory, L2/L1): keeping them
 // out of shared memory leaves room in the SM's combined L1/shared storage
@@ -170,10 +171,10 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 			q = __ldg(record + 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
 			above += v.z > 0.0f ? 1u : 0u;
 			const f3 cur = kChecked ? normalize_checked<P>(v, ok) : normalize<P>(v);
-			r += integrate_edge<P>(prev, cur);
+			r += kChecked ? integrate_edge_checked<P>(prev, cur, ok) : integrate_edge<P>(prev, cur);
 			prev = cur;
 		}
-		r += integrate_edge<P>(prev, first);
+		r += kChecked ? integrate_edge_checked<P>(prev, first, ok) : integrate_edge<P>(prev, first);
 		if (kChecked && !ok) return false;
 		bool a = false;
 		if (above == n) {
