@@ -64,7 +64,9 @@ template <class P> struct BinnedMinBlocks {
 template <> struct BinnedMinBlocks<FastNumerics> {
 	static constexpr int value = RISLTC_BINNED_MIN_BLOCKS_FAST;
 };
-constexpr int kFrameWords = 45;              // 44 used; odd stride avoids bank conflicts
+// A pixel's LTC frame in 11 16-byte words (an odd number of them, so that
+// the 16-byte reads of 8 lanes from different pixels spread over the banks).
+constexpr int kFrameQuads = 11;
 constexpr int kBinnedWarps = 4;              // warps per block
 constexpr int kBins = kMaxLightVertices - 2; // vertex counts 3..8
 
@@ -73,7 +75,7 @@ template <int kSuper, int kPixels, int kChunk> struct WarpTile {
 	static constexpr int kDeferred = kItems + 32;     // deferred items pending at most
 	static_assert(kItems < 1024, "10-bit bin counters");
 	static_assert(kSuper % kChunk == 0 && kPixels * kSuper <= kPHatSlot, "super-chunk layout");
-	float frame[kPixels][kFrameWords];
+	float4 frame[kPixels][kFrameQuads];
 	// Items as light << 10 | slot, slot = pixel lane * kSuper + candidate of
 	// the super-chunk (below 1024; lights below 2^22).
 	uint32_t item[kItems];
@@ -81,29 +83,29 @@ template <int kSuper, int kPixels, int kChunk> struct WarpTile {
 	uint32_t deferred_count;
 };
 
-// Frame layout: position (0-2), diffuse albedo (3-5), LTC albedo (6),
-// world to shading (7-18), world to cosine (19-30) and its y-flipped
-// counterpart (31-42); each mat4x3 column-major.
-RL_DEV void store_frame(float* f, const CandidateFrame& cf) {
-	f[0] = cf.position.x;
-	f[1] = cf.position.y;
-	f[2] = cf.position.z;
-	f[3] = cf.diffuse_albedo.x;
-	f[4] = cf.diffuse_albedo.y;
-	f[5] = cf.diffuse_albedo.z;
-	f[6] = cf.ltc_albedo;
-#pragma unroll
-	for (int c = 0; c != 4; ++c) {
-		f[7 + 3 * c + 0] = cf.w2s.c[c].x;
-		f[7 + 3 * c + 1] = cf.w2s.c[c].y;
-		f[7 + 3 * c + 2] = cf.w2s.c[c].z;
-		f[19 + 3 * c + 0] = cf.w2c[0].c[c].x;
-		f[19 + 3 * c + 1] = cf.w2c[0].c[c].y;
-		f[19 + 3 * c + 2] = cf.w2c[0].c[c].z;
-		f[31 + 3 * c + 0] = cf.w2c[1].c[c].x;
-		f[31 + 3 * c + 1] = cf.w2c[1].c[c].y;
-		f[31 + 3 * c + 2] = cf.w2c[1].c[c].z;
-	}
+// Frame layout (16-byte words): 0 {position, LTC albedo}, 1 {diffuse
+// albedo, 0}, 2-4 world to shading, 5-7 world to cosine, 8-10 its y-flipped
+// counterpart; each mat4x3's 12 floats column-major across three words.
+RL_DEV void store_matrix(float4* q, const mat43& m) {
+	q[0] = make_float4(m.c[0].x, m.c[0].y, m.c[0].z, m.c[1].x);
+	q[1] = make_float4(m.c[1].y, m.c[1].z, m.c[2].x, m.c[2].y);
+	q[2] = make_float4(m.c[2].z, m.c[3].x, m.c[3].y, m.c[3].z);
+}
+RL_DEV mat43 load_matrix(const float4* q) {
+	const float4 a = q[0], b = q[1], c = q[2];
+	mat43 m;
+	m.c[0] = mk3(a.x, a.y, a.z);
+	m.c[1] = mk3(a.w, b.x, b.y);
+	m.c[2] = mk3(b.z, b.w, c.x);
+	m.c[3] = mk3(c.y, c.z, c.w);
+	return m;
+}
+RL_DEV void store_frame(float4* f, const CandidateFrame& cf) {
+	f[0] = make_float4(cf.position.x, cf.position.y, cf.position.z, cf.ltc_albedo);
+	f[1] = make_float4(cf.diffuse_albedo.x, cf.diffuse_albedo.y, cf.diffuse_albedo.z, 0.0f);
+	store_matrix(f + 2, cf.w2s);
+	store_matrix(f + 5, cf.w2c[0]);
+	store_matrix(f + 8, cf.w2c[1]);
 }
 
 // A light vertex (slot j of the record) in local space: mat4x3 * vec4(v, 1)
@@ -139,22 +141,20 @@ __device__ __noinline__ float clipped_integral(mat43 t, const float4* record, ui
 // across the warp.  With allow_clip false, returns false as soon as a space
 // clips the polygon partially; the caller defers the item.
 template <class P, bool kChecked>
-RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+RL_DEV bool binned_candidate(const float4* f, const float4* record, bool allow_clip, float& p_hat) {
 	// kChecked: normalise with normalize_checked and return false (the item
 	// is deferred) if any square root falls outside its range.
 	bool ok = true;
 	const float4 head = __ldg(record), pl = __ldg(record + 1);
 	const uint32_t n = __float_as_uint(head.w);
 	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
-	const bool flip = plane_dot(mk3(f[0], f[1], f[2]), plane) < 0.0f;
+	const float4 f0 = f[0];
+	const bool flip = plane_dot(mk3(f0.x, f0.y, f0.z), plane) < 0.0f;
 	float integral[2];
 	bool away[2];
 #pragma unroll 1
 	for (int s = 0; s != 2; ++s) {
-		const float* m = f + (s == 0 ? 7 : (flip ? 31 : 19));
-		mat43 t;
-#pragma unroll
-		for (int c = 0; c != 4; ++c) t.c[c] = mk3(m[3 * c], m[3 * c + 1], m[3 * c + 2]);
+		const mat43 t = load_matrix(f + (s == 0 ? 2 : (flip ? 8 : 5)));
 		const bool negate_y = s == 0 && flip;
 		float4 q = __ldg(record + 2);
 		f3 v = mul_point(t, mk3(q.x, q.y, q.z));
@@ -198,10 +198,15 @@ RL_DEV bool binned_candidate(const float* f, const float4* record, bool allow_cl
 	}
 	const f3 radiance = mk3(head.x, head.y, head.z);
 	f3 result = splat(0.0f);
-	const f3 diffuse = away[0] ? splat(0.0f) : mul(scale(mk3(f[3], f[4], f[5]), integral[0]), radiance);
+	const float4 f1 = f[1];
+	const f3 diffuse = away[0] ? splat(0.0f) : mul(scale(mk3(f1.x, f1.y, f1.z), integral[0]), radiance);
 	result = add(result, diffuse);
-	const f3 ggx = away[1] ? splat(0.0f) : mul(splat(integral[1] * f[6]), radiance);
+	const f3 ggx = away[1] ? splat(0.0f) : mul(splat(integral[1] * f[0].w), radiance);
 	const f3 color = add(result, ggx);
+	if (kChecked) {
+		p_hat = sqrt_checked<P>(dot(color, color), ok);
+		return ok;
+	}
 	p_hat = P::sqrt(dot(color, color));
 	return true;
 }
@@ -333,22 +338,22 @@ template <class P> RL_DEV float2 integrate_edge2(const f3x2& v1, const f3x2& v2)
 }
 
 template <class P, bool kChecked = false>
-RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+RL_DEV bool binned_candidate_pair(const float4* f, const float4* record, bool allow_clip, float& p_hat) {
 	bool ok = true;
 	const float4 head = __ldg(record), pl = __ldg(record + 1);
 	const uint32_t n = __float_as_uint(head.w);
 	const float plane[4] = {pl.x, pl.y, pl.z, pl.w};
-	const bool flip = plane_dot(mk3(f[0], f[1], f[2]), plane) < 0.0f;
+	const float4 f0 = f[0];
+	const bool flip = plane_dot(mk3(f0.x, f0.y, f0.z), plane) < 0.0f;
 	// Lane .x: world to shading space (y negated on a flip); lane .y: world
 	// to cosine space (the y-flipped matrix on a flip).
-	const float* ms = f + 7;
-	const float* mc = f + (flip ? 31 : 19);
+	const mat43 ms = load_matrix(f + 2), mc = load_matrix(f + (flip ? 8 : 5));
 	mat43x2 t;
 #pragma unroll
 	for (int c = 0; c != 4; ++c) {
-		t.c[c].x = make_float2(ms[3 * c], mc[3 * c]);
-		t.c[c].y = make_float2(ms[3 * c + 1], mc[3 * c + 1]);
-		t.c[c].z = make_float2(ms[3 * c + 2], mc[3 * c + 2]);
+		t.c[c].x = make_float2(ms.c[c].x, mc.c[c].x);
+		t.c[c].y = make_float2(ms.c[c].y, mc.c[c].y);
+		t.c[c].z = make_float2(ms.c[c].z, mc.c[c].z);
 	}
 	// Vertices 0 and 1 first; then iteration j normalises vertex j + 1 while
 	// it integrates edge (j - 1, j), so the two dependency chains overlap.
@@ -399,10 +404,7 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 			rs = 0.0f;
 			a = true;
 		} else {
-			const float* m = s == 0 ? ms : mc;
-			mat43 ts;
-#pragma unroll
-			for (int c = 0; c != 4; ++c) ts.c[c] = mk3(m[3 * c], m[3 * c + 1], m[3 * c + 2]);
+			const mat43 ts = s == 0 ? ms : mc;
 			rs = clipped_integral<P>(ts, record, n, s == 0 && flip);
 			a = rs < 0.0f;
 			rs = a ? 0.0f : rs;
@@ -412,9 +414,10 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 	}
 	const f3 radiance = mk3(head.x, head.y, head.z);
 	f3 result = splat(0.0f);
-	const f3 diffuse = away[0] ? splat(0.0f) : mul(scale(mk3(f[3], f[4], f[5]), integral[0]), radiance);
+	const float4 f1 = f[1];
+	const f3 diffuse = away[0] ? splat(0.0f) : mul(scale(mk3(f1.x, f1.y, f1.z), integral[0]), radiance);
 	result = add(result, diffuse);
-	const f3 ggx = away[1] ? splat(0.0f) : mul(splat(integral[1] * f[6]), radiance);
+	const f3 ggx = away[1] ? splat(0.0f) : mul(splat(integral[1] * f[0].w), radiance);
 	const f3 color = add(result, ggx);
 	p_hat = P::sqrt(dot(color, color));
 	return true;
@@ -427,7 +430,7 @@ RL_DEV bool binned_candidate_pair(const float* f, const float4* record, bool all
 // slower (29.4 against 24.7 ms per 4-frame launch of the candidate kernel).
 // RISLTC_CANDIDATE_PAIRS=1 selects the paired form for exact numerics too.
 template <class P>
-RL_DEV bool evaluate_candidate(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+RL_DEV bool evaluate_candidate(const float4* f, const float4* record, bool allow_clip, float& p_hat) {
 #if RISLTC_CANDIDATE_PAIRS
 	return allow_clip ? binned_candidate_pair<P, false>(f, record, true, p_hat)
 	                  : binned_candidate_pair<P, true>(f, record, false, p_hat);
@@ -439,7 +442,7 @@ RL_DEV bool evaluate_candidate(const float* f, const float4* record, bool allow_
 #endif
 }
 template <>
-RL_DEV bool evaluate_candidate<FastNumerics>(const float* f, const float4* record, bool allow_clip, float& p_hat) {
+RL_DEV bool evaluate_candidate<FastNumerics>(const float4* f, const float4* record, bool allow_clip, float& p_hat) {
 	return binned_candidate_pair<FastNumerics>(f, record, allow_clip, p_hat);
 }
 
