@@ -579,8 +579,7 @@ EXTERN_C int risltc_shade_host(risltc_ctx_t* ctx, const risltc_scene_t* scene, u
  * RISLTC_ERROR_INVALID_ARGUMENT before any work.  The first call on each
  * device resolves the array's device address (cudaGetSymbolAddress) and keeps
  * it for the life of the process; make no call on a device after resetting
- * it (cudaDeviceReset).  The call cannot be captured into a CUDA graph: it
- * copies the error word back and synchronises its stream.  All calls share the array: calls that overlap on the
+ * it (cudaDeviceReset).  All calls share the array: calls that overlap on the
  * GPU (other streams, other threads) race, so serialise them. */
 #define RISLTC_NOALLOC_MAX_PIXEL_FRAMES 262144
 EXTERN_C int risltc_shade_noalloc(const risltc_scene_t* scene, const risltc_gbuffer_t* gbuffer,
