@@ -457,6 +457,11 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 	const uint32_t np = pr.width * pr.height;
 	const int n_lights = pr.scene.light_count;
 	const float p = P::rcp((float) n_lights);
+	// With uniform candidates and a power-of-two light count, p is a power of
+	// two and p_hat / p equals p_hat * (1 / p) bit for bit (scaling by a
+	// power of two is exact): the replay multiplies instead of dividing.
+	const bool scale_weight = !pr.candidates && (n_lights & (n_lights - 1)) == 0;
+	const float inv_p = (float) n_lights;
 	// Lanes kPixels..31 own no pixel: they draw nothing and only evaluate
 	// items of the sorted lists.
 	const bool own = lane < (uint32_t) kPixels;
@@ -609,7 +614,7 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 						}
 						const float rnd = get_noise_1(seed);
 						const float p_hat = phat[lane * kSuper + k];
-						const float w = P::div(p_hat, pk);
+						const float w = scale_weight ? p_hat * inv_p : P::div(p_hat, pk);
 						if (pr.train_stride && f == 0 && i % pr.train_stride == pr.train_phase)
 							pr.train_candidates[(size_t) i * pr.candidate_count + cs + k].pdf = w;
 						w_sum += w;
