@@ -43,7 +43,8 @@ struct risltc_ctx_s {
 	// The binned candidate kernel's per-warp p_hat slots: one region per
 	// stream that may run it at the same time (the context's stream and the
 	// batch streams share regions 0..RISLTC_BATCH_STREAMS-1), each with a slot
-	// per warp of the largest grid (sm_count * 16 blocks of 4 warps).
+	// per warp of the largest grid (sm_count * kCandidateBlocksPerSm blocks of
+	// 4 warps).
 	float* d_phat;
 	int phat_regions;
 	// Proposal candidates (light, pdf) per pixel-frame and candidate.
@@ -734,7 +735,7 @@ int reserve_candidates(risltc_ctx_t* ctx, size_t need) {
 }
 
 size_t phat_region_floats(const risltc_ctx_t* ctx) {
-	return (size_t) ctx->sm_count * 16 * risltc::kBinnedWarps * risltc::kPHatSlot;
+	return (size_t) ctx->sm_count * risltc::kCandidateBlocksPerSm * risltc::kBinnedWarps * risltc::kPHatSlot;
 }
 
 int reserve_phat(risltc_ctx_t* ctx, int regions) {

@@ -41,11 +41,15 @@ namespace risltc {
 #define RISLTC_BINNED_MIN_BLOCKS_FAST 4
 #endif
 
-// A warp's p_hat values of one super-chunk, [pixel lane][candidate], live in
-// its slot of RisParams::p_hat_scratch (global memory, L2/L1): keeping them
-// out of shared memory leaves room in the SM's combined L1/shared storage
-// for the light records the candidates read.
-constexpr int kPHatSlot = 32 * 32;
+// A warp's p_hat values, [window unit][pixel lane][candidate], live in its
+// slot of RisParams::p_hat_scratch (global memory, L2/L1): keeping them out
+// of shared memory leaves room in the SM's combined L1/shared storage for
+// the light records the candidates read.  A slot holds 4096 values: four
+// 32-pixel super-chunks of 32 candidates in the default tile.
+constexpr int kPHatSlot = 4096;
+// The candidate kernels run at most this many blocks per SM (their grid is
+// one resident wave); the p_hat scratch has a slot per warp of such a grid.
+constexpr int kCandidateBlocksPerSm = 8;
 
 // Candidates per pixel per super-chunk (measured best: 32 in exact numerics,
 // 16 in fast numerics, where the smaller tile leaves more L1 for the lights).
@@ -74,12 +78,13 @@ template <int kSuper, int kPixels, int kChunk> struct WarpTile {
 	static constexpr int kItems = kPixels * kChunk;  // items per warp per chunk
 	static constexpr int kDeferred = kItems + 32;     // deferred items pending at most
 	static_assert(kItems < 1024, "10-bit bin counters");
-	static_assert(kSuper % kChunk == 0 && kPixels * kSuper <= kPHatSlot, "super-chunk layout");
+	static_assert(kSuper % kChunk == 0 && kPixels * kSuper <= 1024, "super-chunk layout (10-bit slots)");
 	float4 frame[kPixels][kFrameQuads];
 	// Items as light << 10 | slot, slot = pixel lane * kSuper + candidate of
 	// the super-chunk (below 1024; lights below 2^22).
 	uint32_t item[kItems];
 	uint32_t deferred[kDeferred];
+	uint8_t deferred_unit[kDeferred];  // the window unit of each deferred item
 	uint32_t deferred_count;
 };
 
@@ -492,19 +497,37 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 		}
 		__syncwarp();
 		const uint32_t x = i % pr.width, y = i / pr.width;
-		for (uint32_t f = 0; f != pr.frame_count; ++f) {
-			uint32_t seed = 0;
-			if (valid) {
-				const uint32_t rn_x = pr.animate ? wang_random_number((pr.noise_seed + f) * 4u) : 0u;
-				seed = get_noise_accessor(x, y, pr.width, rn_x);
-			}
-			float w_sum = 0.0f, sample_value = 0.0f;
-			int res_index = -1;
-			for (int cs = 0; cs < pr.candidate_count; cs += kSuper) {
-				const int super_count = min(kSuper, pr.candidate_count - cs);
-				uint32_t draw = seed;
-				if (lane == 0) tile.deferred_count = 0;
-				__syncwarp();
+		// The noise state at the start of frame f (get_noise_accessor with
+		// the frame's random offset).
+		auto frame_seed = [&](uint32_t f) -> uint32_t {
+			if (!valid) return 0u;
+			const uint32_t rn_x = pr.animate ? wang_random_number((pr.noise_seed + f) * 4u) : 0u;
+			return get_noise_accessor(x, y, pr.width, rn_x);
+		};
+		// The tile's work comes in units of one frame's super-chunk.  Up to
+		// kWindow units are evaluated before their reservoirs are replayed, so
+		// that deferred items of several units share the general path's
+		// rounds: unit u of the window keeps its p_hat values at
+		// phat[u * kUnitSlots + slot].
+		constexpr uint32_t kUnitSlots = (uint32_t) (kPixels * kSuper);
+		constexpr uint32_t kWindow = (uint32_t) kPHatSlot / kUnitSlots;
+		const uint32_t units_per_frame = ((uint32_t) pr.candidate_count + kSuper - 1) / kSuper;
+		const uint32_t units = pr.frame_count * units_per_frame;
+		// The replay's cursor: frame rf, its next super-chunk rcs, and the
+		// frame's reservoir so far.
+		uint32_t rf = 0, rcs = 0, seed = 0;
+		float w_sum = 0.0f, sample_value = 0.0f;
+		int res_index = -1;
+		uint32_t window = 0;  // units evaluated since the last replay
+		uint32_t draw = 0;    // the draw phase's noise state
+		if (lane == 0) tile.deferred_count = 0;
+		__syncwarp();
+		for (uint32_t unit = 0; unit != units; ++unit) {
+			const uint32_t f = unit / units_per_frame, cs = (unit % units_per_frame) * kSuper;
+			if (cs == 0) draw = frame_seed(f);
+			const int super_count = min(kSuper, pr.candidate_count - (int) cs);
+			float* const uphat = phat + window * kUnitSlots;
+			{
 				for (int c0 = 0; c0 < super_count; c0 += kChunk) {
 					const int chunk = min(kChunk, super_count - c0);
 					// 1. This lane's candidate lights; bin them by vertex count
@@ -558,8 +581,8 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 					}
 					__syncwarp();
 					// 3. Evaluate the sorted items, 32 at a time; defer partial
-					//    clips, and evaluate deferred items whenever 32 are
-					//    pending.
+					//    clips (with their unit), and evaluate deferred items
+					//    whenever 32 are pending.
 					for (uint32_t base = 0; base < item_count; base += 32) {
 						const uint32_t it = base + lane;
 						if (it < item_count) {
@@ -568,10 +591,11 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 							const int32_t l = (int32_t) (item >> 10);
 							float ph;
 							if (evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, l), false, ph)) {
-								phat[slot] = ph;
+								uphat[slot] = ph;
 							} else {
 								const uint32_t d = atomicAdd(&tile.deferred_count, 1u);
 								tile.deferred[d] = item;
+								tile.deferred_unit[d] = (uint8_t) window;
 							}
 						}
 					}
@@ -582,41 +606,56 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 						float ph = 0.0f;
 						evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[d] >> 10)),
 						                      true, ph);
-						phat[slot] = ph;
+						phat[tile.deferred_unit[d] * kUnitSlots + slot] = ph;
 						__syncwarp();
 						if (lane == 0) tile.deferred_count = pending - 32;
 						__syncwarp();
 					}
 				}
-				// The rest of the deferred items.
-				const uint32_t rest = tile.deferred_count;
-				if (lane < rest) {
-					const uint32_t slot = tile.deferred[lane] & 1023u;
-					float ph = 0.0f;
-					evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[lane] >> 10)),
-					                      true, ph);
-					phat[slot] = ph;
+			}
+			++window;
+			if (window != kWindow && unit + 1 != units) continue;
+			// The window's remaining deferred items.
+			const uint32_t rest = tile.deferred_count;
+			if (lane < rest) {
+				const uint32_t slot = tile.deferred[lane] & 1023u;
+				float ph = 0.0f;
+				evaluate_candidate<P>(tile.frame[slot / kSuper], light_record(pr.scene, (int) (tile.deferred[lane] >> 10)),
+				                      true, ph);
+				phat[tile.deferred_unit[lane] * kUnitSlots + slot] = ph;
+			}
+			__syncwarp();
+			if (lane == 0) tile.deferred_count = 0;
+			__syncwarp();
+			// 4. Reservoir updates of the window's units in candidate order,
+			//    drawing the same noise again; a frame's record is written
+			//    after its last super-chunk.
+			for (uint32_t u = 0; u != window; ++u) {
+				if (rcs == 0) {
+					seed = frame_seed(rf);
+					w_sum = 0.0f;
+					sample_value = 0.0f;
+					res_index = -1;
 				}
-				__syncwarp();
-				// 4. Reservoir updates in candidate order, drawing the same
-				//    noise again.
+				const int rcount = min(kSuper, pr.candidate_count - (int) rcs);
+				const float* const rphat = phat + u * kUnitSlots + lane * kSuper;
 				if (valid) {
 #pragma unroll 4
-					for (int k = 0; k < super_count; ++k) {
+					for (int k = 0; k < rcount; ++k) {
 						int idx = (int) (get_noise_1(seed) * (float) n_lights);
 						idx = idx > n_lights - 1 ? n_lights - 1 : idx;
 						float pk = p;
 						if (pr.candidates) {
 							const ProposalCandidate q =
-							    pr.candidates[((size_t) f * np + i) * pr.candidate_count + cs + k];
+							    pr.candidates[((size_t) rf * np + i) * pr.candidate_count + rcs + k];
 							idx = q.light;
 							pk = q.pdf;
 						}
 						const float rnd = get_noise_1(seed);
-						const float p_hat = phat[lane * kSuper + k];
+						const float p_hat = rphat[k];
 						const float w = scale_weight ? p_hat * inv_p : P::div(p_hat, pk);
-						if (pr.train_stride && f == 0 && i % pr.train_stride == pr.train_phase)
-							pr.train_candidates[(size_t) i * pr.candidate_count + cs + k].pdf = w;
+						if (pr.train_stride && rf == 0 && i % pr.train_stride == pr.train_phase)
+							pr.train_candidates[(size_t) i * pr.candidate_count + rcs + k].pdf = w;
 						w_sum += w;
 						if (w > 0.0f && rnd < P::div(w, w_sum)) {
 							res_index = idx;
@@ -624,12 +663,18 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 						}
 					}
 				}
-				__syncwarp();
+				rcs += kSuper;
+				if (rcs >= (uint32_t) pr.candidate_count) {
+					if (valid)
+						pr.records[(size_t) rf * np + i] = ReservoirRecord{res_index, w_sum, sample_value, seed};
+					else if (own && i < np)
+						pr.records[(size_t) rf * np + i] = ReservoirRecord{-1, 0.0f, 0.0f, 0u};
+					++rf;
+					rcs = 0;
+				}
 			}
-			if (valid)
-				pr.records[(size_t) f * np + i] = ReservoirRecord{res_index, w_sum, sample_value, seed};
-			else if (own && i < np)
-				pr.records[(size_t) f * np + i] = ReservoirRecord{-1, 0.0f, 0.0f, 0u};
+			window = 0;
+			__syncwarp();
 		}
 		__syncwarp();
 	}
@@ -670,7 +715,7 @@ cudaError_t configure_candidate_kernel(Kernel kernel, size_t smem, std::atomic<u
 	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * kBinnedWarps, smem);
 	if (e != cudaSuccess) return e;
-	resident[device & 63].store(std::max(1, sms * per_sm));
+	resident[device & 63].store(std::max(1, sms * std::min(per_sm, kCandidateBlocksPerSm)));
 	configured.fetch_or(bit);
 	return cudaSuccess;
 }
