@@ -122,15 +122,39 @@ RL_DEV f3 local_vertex(const mat43& t, const float4* record, uint32_t j, bool ne
 	return v;
 }
 
-// The partially clipped case: clip_polygon, then calculate_ltc; -1 when the
-// polygon clips to nothing.  Kept out of line (about 1% of candidates).
-template <class P>
-__device__ __noinline__ float clipped_integral(mat43 t, const float4* record, uint32_t n, bool negate_y) {
-	f3 v[kMaxPolygonVertices];
-#pragma unroll
-	for (int j = 0; j != kMaxLightVertices; ++j) v[j] = local_vertex(t, record, (uint32_t) j, negate_y);
-	const uint32_t vc = clip_polygon<P>(n, v);
-	return vc > 0 ? calculate_ltc<P>(vc, v) : -1.0f;
+// The partially clipped case, streamed: the integral calculate_ltc gives
+// over the polygon clip_polygon makes (mask: the vertices above z = 0, one
+// bit each), with the clipped vertices produced one at a time in the order of
+// clip_polygon's output slots: the cycle [entry, the run above the horizon,
+// exit] starting at its rotation, the run's vertices transformed again from
+// the light record.  The same values in the same order as clip_polygon
+// followed by calculate_ltc, without a vertex array.  -1 when the polygon
+// clips to nothing.  With kChecked, uses the branch-free normalisation and
+// edge integral and clears ok where they do not apply.
+template <class P, bool kChecked>
+RL_DEV float clipped_integral(const mat43& t, const float4* record, uint32_t n, bool negate_y, uint32_t mask, bool& ok) {
+	const uint32_t k = __popc(mask);
+	const uint32_t s = clip_run_start(n, mask);
+	if (s == n) return -1.0f;
+	const uint32_t e = clip_wrap(s + k - 1, n), vc = k + 2;
+	const f3 entry = iz0<P>(local_vertex(t, record, clip_wrap(s + n - 1, n), negate_y), local_vertex(t, record, s, negate_y));
+	const f3 exit = iz0<P>(local_vertex(t, record, e, negate_y), local_vertex(t, record, clip_wrap(e + 1, n), negate_y));
+	const uint32_t j0 = clip_wrap(vc - clip_rotation(n, k, s), vc);  // cycle element of slot 0
+	f3 first = splat(0.0f), prev = splat(0.0f);
+	float r = 0.0f;
+#pragma unroll 1
+	for (uint32_t slot = 0; slot != vc; ++slot) {
+		const uint32_t j = clip_wrap(j0 + slot, vc);
+		const f3 v = j == 0 ? entry : (j == k + 1 ? exit : local_vertex(t, record, clip_wrap(s + j - 1, n), negate_y));
+		const f3 cur = kChecked ? normalize_checked<P>(v, ok) : normalize<P>(v);
+		if (slot == 0)
+			first = cur;
+		else
+			r += kChecked ? integrate_edge_checked<P>(prev, cur, ok) : integrate_edge<P>(prev, cur);
+		prev = cur;
+	}
+	r += kChecked ? integrate_edge_checked<P>(prev, first, ok) : integrate_edge<P>(prev, first);
+	return fabsf(r);
 }
 
 // One candidate (ltc_cp_candidate, then p_hat = length(color)) with the
@@ -165,7 +189,7 @@ RL_DEV bool binned_candidate(const float4* f, const float4* record, bool allow_c
 		f3 v = mul_point(t, mk3(q.x, q.y, q.z));
 		v.y = negate_y ? -v.y : v.y;
 		q = __ldg(record + 3);
-		uint32_t above = v.z > 0.0f ? 1u : 0u;
+		uint32_t mask = v.z > 0.0f ? 1u : 0u;  // bit j: vertex j above the horizon
 		const f3 first = kChecked ? normalize_checked<P>(v, ok) : normalize<P>(v);
 		f3 prev = first;
 		float r = 0.0f;
@@ -174,7 +198,7 @@ RL_DEV bool binned_candidate(const float4* f, const float4* record, bool allow_c
 			v = mul_point(t, mk3(q.x, q.y, q.z));
 			v.y = negate_y ? -v.y : v.y;
 			q = __ldg(record + 2 + min(j + 1, (uint32_t) kMaxLightVertices - 1));
-			above += v.z > 0.0f ? 1u : 0u;
+			mask |= (v.z > 0.0f ? 1u : 0u) << j;
 			const f3 cur = kChecked ? normalize_checked<P>(v, ok) : normalize<P>(v);
 			r += kChecked ? integrate_edge_checked<P>(prev, cur, ok) : integrate_edge<P>(prev, cur);
 			prev = cur;
@@ -182,14 +206,15 @@ RL_DEV bool binned_candidate(const float4* f, const float4* record, bool allow_c
 		r += kChecked ? integrate_edge_checked<P>(prev, first, ok) : integrate_edge<P>(prev, first);
 		if (kChecked && !ok) return false;
 		bool a = false;
-		if (above == n) {
+		if (mask == (1u << n) - 1u) {
 			r = fabsf(r);
-		} else if (above == 0) {
+		} else if (mask == 0) {
 			r = 0.0f;
 			a = true;
 		} else {
 			if (!allow_clip) return false;
-			r = clipped_integral<P>(t, record, n, negate_y);
+			r = clipped_integral<P, kChecked>(t, record, n, negate_y, mask, ok);
+			if (kChecked && !ok) return false;
 			a = r < 0.0f;
 			r = a ? 0.0f : r;
 		}
@@ -368,12 +393,12 @@ RL_DEV bool binned_candidate_pair(const float4* f, const float4* record, bool al
 	float4 q = __ldg(record + 4);
 	f3x2 v = mul_point2<P>(t, q0);
 	if (flip) v.y.x = -v.y.x;
-	uint32_t above_s = v.z.x > 0.0f ? 1u : 0u, above_c = v.z.y > 0.0f ? 1u : 0u;
+	uint32_t above_s = v.z.x > 0.0f ? 1u : 0u, above_c = v.z.y > 0.0f ? 1u : 0u;  // bit j: vertex j above
 	const f3x2 first = kChecked ? normalize2_checked<P>(v, ok) : normalize2<P>(v);
 	v = mul_point2<P>(t, q1);
 	if (flip) v.y.x = -v.y.x;
-	above_s += v.z.x > 0.0f ? 1u : 0u;
-	above_c += v.z.y > 0.0f ? 1u : 0u;
+	above_s |= (v.z.x > 0.0f ? 1u : 0u) << 1;
+	above_c |= (v.z.y > 0.0f ? 1u : 0u) << 1;
 	f3x2 prev = first, cur = kChecked ? normalize2_checked<P>(v, ok) : normalize2<P>(v);
 	float2 r = pair(0.0f);
 #pragma unroll kPairUnroll
@@ -383,8 +408,8 @@ RL_DEV bool binned_candidate_pair(const float4* f, const float4* record, bool al
 			v = mul_point2<P>(t, q);
 			if (flip) v.y.x = -v.y.x;
 			q = __ldg(record + 2 + min(j + 2, (uint32_t) kMaxLightVertices - 1));
-			above_s += v.z.x > 0.0f ? 1u : 0u;
-			above_c += v.z.y > 0.0f ? 1u : 0u;
+			above_s |= (v.z.x > 0.0f ? 1u : 0u) << (j + 1);
+			above_c |= (v.z.y > 0.0f ? 1u : 0u) << (j + 1);
 			next = kChecked ? normalize2_checked<P>(v, ok) : normalize2<P>(v);
 		}
 		r = padd<P>(r, integrate_edge2<P>(prev, cur));
@@ -393,7 +418,8 @@ RL_DEV bool binned_candidate_pair(const float4* f, const float4* record, bool al
 	}
 	r = padd<P>(r, integrate_edge2<P>(prev, first));
 	if (kChecked && !ok) return false;
-	const bool partial_s = above_s != n && above_s != 0, partial_c = above_c != n && above_c != 0;
+	const uint32_t all = (1u << n) - 1u;
+	const bool partial_s = above_s != all && above_s != 0, partial_c = above_c != all && above_c != 0;
 	if ((partial_s || partial_c) && !allow_clip) return false;
 	float integral[2];
 	bool away[2];
@@ -403,14 +429,15 @@ RL_DEV bool binned_candidate_pair(const float4* f, const float4* record, bool al
 	for (int s = 0; s != 2; ++s) {
 		float rs = sum[s];
 		bool a = false;
-		if (above[s] == n) {
+		if (above[s] == all) {
 			rs = fabsf(rs);
 		} else if (above[s] == 0) {
 			rs = 0.0f;
 			a = true;
 		} else {
 			const mat43 ts = s == 0 ? ms : mc;
-			rs = clipped_integral<P>(ts, record, n, s == 0 && flip);
+			bool unused = true;
+			rs = clipped_integral<P, false>(ts, record, n, s == 0 && flip, above[s], unused);
 			a = rs < 0.0f;
 			rs = a ? 0.0f : rs;
 		}
@@ -442,8 +469,10 @@ RL_DEV bool evaluate_candidate(const float4* f, const float4* record, bool allow
 #else
 	// The first pass (allow_clip false) takes the branch-free square root;
 	// deferred items are evaluated with the general one.
-	return allow_clip ? binned_candidate<P, false>(f, record, true, p_hat)
-	                  : binned_candidate<P, true>(f, record, false, p_hat);
+	if (!allow_clip) return binned_candidate<P, true>(f, record, false, p_hat);
+	// Deferred items: the branch-free forms where they apply (every item
+	// seen so far), the general ones otherwise.
+	return binned_candidate<P, true>(f, record, true, p_hat) || binned_candidate<P, false>(f, record, true, p_hat);
 #endif
 }
 template <>
