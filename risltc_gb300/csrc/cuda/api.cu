@@ -323,7 +323,8 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 	for (size_t i = 0; i != 9 * (size_t) triangle_count; ++i)
 		if (!std::isfinite(triangles[i])) return RISLTC_ERROR_NON_FINITE;
 	cudaSetDevice(ctx->device);
-	// Lights: 160-byte records {radiance, vertex_count | plane | 8 x {xyz, 0}}.
+	// Lights: 160-byte records {radiance, vertex_count | plane | 8 x {xyz, 0}},
+	// then the vertex counts as bytes.
 	const size_t stride = 12 + 4 * (size_t) max_vertex_count;
 	std::vector<float> lights((size_t) light_count * risltc::kLightWords, 0.0f);
 	for (uint32_t i = 0; i != light_count; ++i) {
@@ -373,6 +374,19 @@ EXTERN_C int risltc_scene_create(risltc_ctx_t* ctx, const float* lights_std140, 
 		e = cudaMalloc(dst, bytes);
 		if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
 	};
+	{
+		// After the records, one byte per light with its vertex count: the
+		// candidate kernel bins its draws by vertex count from this 16 KB
+		// table (16,384 lights) instead of each record's first sector.
+		const size_t records = lights.size();
+		lights.resize(records + (light_count + 3) / 4, 0.0f);
+		uint8_t* counts = reinterpret_cast<uint8_t*>(lights.data() + records);
+		for (uint32_t i = 0; i != light_count; ++i) {
+			uint32_t vc;
+			memcpy(&vc, lights.data() + (size_t) i * risltc::kLightWords + 3, 4);
+			counts[i] = (uint8_t) vc;
+		}
+	}
 	upload(&scene->d_lights, lights.data(), lights.size() * sizeof(float));
 	upload(&scene->d_ltc, ltc_dev.data(), ltc_dev.size() * sizeof(float));
 	if (triangle_count) {

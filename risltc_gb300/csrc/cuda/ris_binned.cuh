@@ -575,7 +575,7 @@ RL_DEV void binned_tile(const RisParams& pr, WarpTile<BinnedSuper<P>::value, kPi
 								idx = pr.candidates[((size_t) f * np + i) * pr.candidate_count + cs + c0 + k].light;
 							get_noise_1(draw);
 							light[k] = idx;
-							bin[k] = __float_as_uint(__ldg(light_record(pr.scene, idx)).w) - 3u;
+							bin[k] = light_vertex_count(pr.scene, idx) - 3u;
 							counts += 1ull << (10 * bin[k]);
 						}
 					}
