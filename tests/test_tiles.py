@@ -44,7 +44,12 @@ def render(env, s, frames=2, seed=11):
 
 
 @pytest.mark.parametrize("numerics", ["exact", "fast"])
-@pytest.mark.parametrize("candidates", [32, 13, 8])
+# 40 and 96 candidates take two and three super-chunks per frame, so the
+# binned kernels' windows of deferred items and replays (four 32-candidate
+# super-chunks in exact numerics, eight 16-candidate ones in fast numerics)
+# end in the middle of a frame; the per-pixel kernel evaluates each pixel's
+# candidates in sequence and checks that bookkeeping independently.
+@pytest.mark.parametrize("candidates", [32, 13, 8, 40, 96])
 def test_every_tile_equals_the_default(env, numerics, candidates):
     rl = env[0]
     rgb0, res0 = render(env, rl.settings(candidates=candidates, numerics=numerics))
