@@ -12,13 +12,16 @@
 //      with a counting sort over the warp, so that the lanes of one step
 //      mostly evaluate polygons with the same number of vertices;
 //   3. evaluates the items with each pixel's LTC frame read from shared
-//      memory; an item whose polygon is partially clipped in either space is
-//      deferred to a list that the warp evaluates 32 at a time, so the slow
-//      clipping path runs with full warps.
-// At the end of the super-chunk the last deferred items are evaluated and
+//      memory, in a form without branches (correctly rounded square roots
+//      from sqrt_tuckerman); an item whose polygon is partially clipped in
+//      either space, or outside that form's range, is deferred to a list
+//      that the warp evaluates 32 at a time, so the clipping path runs with
+//      full warps.
+// A frame's super-chunk is a unit; after up to four units (a window) the
+// last deferred items of the window are evaluated and
 //   4. each lane replays its pixel's reservoir updates in candidate order
-//      (insert_in_reservoir, reservoir.glsl:34-41), drawing the same noise
-//      again.
+//      (insert_in_reservoir, reservoir.glsl:34-41), unit by unit, drawing the
+//      same noise again.
 // Every p_hat is computed by the same operations on the same values as in
 // ris_candidates_kernel and the reservoir sees them in the same order, so the
 // reservoir records are bit-identical.
