@@ -114,3 +114,38 @@ def test_closing_the_context_first_destroys_its_scenes_and_models(rl):
     scene.close()
     model.close()
     del scene, model, ctx
+
+
+def test_large_lights_close_to_the_surface(rl):
+    """Large triangles and quads just above the surface: seen from the pixels
+    below them, consecutive vertices lie 90 degrees or more apart and many
+    polygons straddle the horizon, so the candidate kernel's branch-free
+    first pass defers these items, and the deferred items' own branch-free
+    pass falls back to the general path.  Bit for bit the oracle's frame."""
+    import risltc_gb300 as rlm
+    sc = heightfield(48, 27, 4, 600, seed=12)
+    covered = sc["primitive"] == 0
+    pos = sc["gbuffer"][0:3].T[covered].astype(np.float64)
+    top = float(pos[:, 2].max()) + 0.05
+    rng = np.random.default_rng(13)
+    specs = []
+    for k in range(24):
+        n = 3 + k % 3
+        ang = 2.0 * np.pi * np.arange(n) / n + rng.uniform(0.0, 2.0 * np.pi)
+        verts = np.stack([np.cos(ang), np.sin(ang)], axis=1)
+        c = pos[rng.integers(len(pos))]
+        specs.append(rlm.scenes.LightSpec((np.pi + rng.uniform(-0.2, 0.2), rng.uniform(-0.2, 0.2), 0.0),
+                                          (rng.uniform(1.5, 3.0),) * 2, (c[0], c[1], top + rng.uniform(0.0, 0.1)),
+                                          tuple(np.exp(rng.uniform(np.log(0.5), np.log(5.0), 3))), verts))
+    sc["lights"], sc["max_vertex_count"] = rlm.scenes.build_lights(specs)
+    # The geometry does what the test is for: some pixel sees two consecutive
+    # vertices of some light 90 degrees or more apart.
+    nv = sc["lights"][:, 8].view(np.uint32)
+    world = sc["lights"][:, 12:].reshape(len(specs), -1, 4)[:, :, :3].astype(np.float64)
+    obtuse = False
+    for li in range(len(specs)):
+        d = world[li, :nv[li]][None, :, :] - pos[:, None, :]
+        d /= np.linalg.norm(d, axis=2, keepdims=True)
+        obtuse |= bool((np.sum(d * np.roll(d, -1, axis=1), axis=2) <= 0.0).any())
+    assert obtuse
+    check_bit_exact(rl, sc, 32)
