@@ -17,6 +17,7 @@ in one launch of each kernel).  The line reports:
                plain RIS and the heuristic cluster proposal;
   parity       the GPU's frame against the oracle on the CPU-baseline
                sample (bit-exact pixels expected);
+  rates        candidates per second and shadow rays per second;
   roofline, cpu_baseline, clocks, gpu_launches, kernels, config2 (the
                1024-light, 200k-occluder frame's throughput).
 
@@ -432,7 +433,7 @@ def measure_throughput(a, rl, torch, ctx, fr, rank, world, local_rank, dist, ste
     elapsed = float(t.item())
     res = {"value": samples_per_step * world * steps / elapsed / 1e9, "ms_per_step": 1000.0 * elapsed / steps,
            "elapsed": elapsed, "samples_per_step": samples_per_step, "gpu_launches": launches, "prof": prof,
-           "clocks": clock_info, "flushed": flush is not None}
+           "clocks": clock_info, "flushed": flush is not None, "rays_per_step": ctx.ray_count()}
     # The same step with the other numerics mode, for reference (exact is
     # bit-identical to the oracle; fast approximates the candidate loop).
     other = "fast" if a.numerics == "exact" else "exact"
@@ -523,6 +524,17 @@ def attach_dram(kernels, workload, samples_per_step, peaks):
             if peaks.get("hbm_gbs"):
                 k["dram_frac_of_hbm"] = k["dram_gbs"] / peaks["hbm_gbs"]
             k["dram_source"] = source
+
+
+def rates_of(a, thr, kernels):
+    """Candidates per second (M per pixel-sample) and shadow rays per second
+    (the rays of the last timed call, which risltc_ctx_ray_count reports)
+    over the step and over the trace kernel's own time."""
+    rays = thr.get("rays_per_step") or 0
+    trace = kernels.get("shadow_trace_kernel", {}).get("ms_per_launch")
+    return {"gcandidates_per_s": thr["value"] * a.candidates, "shadow_rays_per_step": rays,
+            "grays_per_s_step": rays / (thr["ms_per_step"] / 1e3) / 1e9 if rays else None,
+            "grays_per_s_trace_kernel": rays / (trace / 1e3) / 1e9 if rays and trace else None}
 
 
 def roofline_of(kernels, fp32_peak, flops_per_sample, samples_per_step, ms_per_step, sms, sm_max, workload):
@@ -765,6 +777,7 @@ def run_ours(a, rank, world, local_rank):
     line.update({
         "config": config_of(a, hs, thr, world),
         "gpu_launches": thr["gpu_launches"],
+        "rates": rates_of(a, thr, kernels),
         "kernels": kernels,
         "other_numerics": thr["other_numerics"],
         "roofline": roofline,

@@ -612,6 +612,14 @@ EXTERN_C int risltc_ctx_profile(risltc_ctx_t* ctx, int enable, float* phase_ms, 
  * memory copies and sets excluded). */
 EXTERN_C int risltc_ctx_launch_count(const risltc_ctx_t* ctx, uint64_t* launches);
 
+/* The shadow rays that the last risltc_shade call on the context traced
+ * through its ray queue (the default configuration with shadows on: rays
+ * grouped by light, then traced by the persistent kernel); 0 when that call
+ * traced none that way.  Waits for the context's stream.  No counterpart in
+ * the reference, whose ray queries run inside the fragment shader; the
+ * shadow-ray rate of the benchmark (rays per second) comes from it. */
+EXTERN_C int risltc_ctx_ray_count(risltc_ctx_t* ctx, uint32_t* rays);
+
 /* Synchronises the context's stream and returns the first error recorded by
    a kernel since the last check (RISLTC_OK if none). */
 EXTERN_C int risltc_ctx_check(risltc_ctx_t* ctx);

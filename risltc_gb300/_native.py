@@ -169,6 +169,7 @@ SIGNATURES = {
                                            ctypes.c_void_p]),
     "risltc_ctx_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_float_p, c_u32_p]),
     "risltc_ctx_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "risltc_ctx_ray_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)]),
     "risltc_ctx_check": (ctypes.c_int, [ctypes.c_void_p]),
     "risltc_ctx_inject_fault": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
     "risltc_status_string": (ctypes.c_char_p, [ctypes.c_int]),

@@ -122,6 +122,13 @@ class Context:
         check(self._lib.risltc_ctx_launch_count(self._h, ctypes.byref(n)), "risltc_ctx_launch_count")
         return int(n.value)
 
+    def ray_count(self):
+        """risltc_ctx_ray_count: shadow rays the last risltc_shade call traced
+        through its ray queue (0 if it traced none that way)."""
+        n = ctypes.c_uint32(0)
+        check(self._lib.risltc_ctx_ray_count(self._h, ctypes.byref(n)), "risltc_ctx_ray_count")
+        return int(n.value)
+
     def close(self):
         if self._h:
             for destroy, handle in reversed(self._owned):

@@ -82,6 +82,9 @@ struct risltc_ctx_s {
 	cudaEvent_t events[64][RISLTC_PROFILE_PHASES + 1];
 	// Kernels of this library launched through the context (risltc_ctx_launch_count).
 	uint64_t kernel_launches;
+	// Whether the last risltc_shade call queued its shadow rays (queue 0 of
+	// d_ray_count then holds their number: risltc_ctx_ray_count).
+	int rays_queued;
 	int events_created;
 };
 
@@ -950,8 +953,10 @@ int shade_on_context(risltc_ctx_t* ctx, const risltc_scene_t* scene, const rislt
 	}
 	const Scratch sc{ctx->d_records, ctx->d_phat, ctx->d_candidates, ctx->d_logits, ctx->d_samples, ctx->d_staged,
 	                 ctx->d_rays, ctx->d_hits, ctx->d_ray_count, ctx->d_light_rays};
-	return shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise_seed, animate, frame_count, out_rgb, accum,
-	                 reservoirs, events);
+	st = shade_one(ctx, ctx->stream, sc, scene, gbuffer, settings, noise_seed, animate, frame_count, out_rgb, accum,
+	               reservoirs, events);
+	ctx->rays_queued = st == RISLTC_OK && uses_ris_pipeline(settings) && uses_ray_queue(scene, settings, pixel_frames);
+	return st;
 }
 
 }  // namespace
@@ -1334,6 +1339,16 @@ EXTERN_C int risltc_trace_shadow(risltc_ctx_t* ctx, const risltc_scene_t* scene,
 	cudaError_t e = risltc::launch_trace_exact(scene->view, (const float4*) rays, ray_count, hits, ctx->d_error,
 	                                           ctx->stream, grid_for(ctx, ray_count));
 	if (e == cudaSuccess) ctx->kernel_launches += 1;
+	return cuda_status(e);
+}
+
+EXTERN_C int risltc_ctx_ray_count(risltc_ctx_t* ctx, uint32_t* rays) {
+	if (!ctx || !rays) return RISLTC_ERROR_INVALID_ARGUMENT;
+	*rays = 0;
+	if (!ctx->rays_queued || !ctx->d_ray_count) return RISLTC_OK;
+	cudaSetDevice(ctx->device);
+	cudaError_t e = cudaMemcpyAsync(rays, ctx->d_ray_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
 	return cuda_status(e);
 }
 

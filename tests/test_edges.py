@@ -149,3 +149,27 @@ def test_large_lights_close_to_the_surface(rl):
         obtuse |= bool((np.sum(d * np.roll(d, -1, axis=1), axis=2) <= 0.0).any())
     assert obtuse
     check_bit_exact(rl, sc, 32)
+
+
+def test_ray_count_of_the_last_call(rl):
+    """risltc_ctx_ray_count reports the shadow rays the last call traced
+    through its ray queue: at most two per covered pixel-frame, the same for
+    the same noise, none without shadows."""
+    rlm, ctx, torch = rl
+    sc = heightfield(64, 36, 48, 800, seed=14)
+    l0, l1, k = gd.ltc()
+    scene = rlm.Scene(ctx, sc["lights"], sc["max_vertex_count"], l0, l1, k, sc["triangles"])
+    g = torch.from_numpy(sc["gbuffer"]).cuda()
+    prim = torch.from_numpy(sc["primitive"].view(np.int32)).cuda()
+    out = torch.zeros((sc["width"] * sc["height"], 3), device="cuda")
+    counts = []
+    for shadows in (True, True, False):
+        rlm.shade(ctx, scene, g, sc["width"], sc["height"], rlm.settings(candidates=8, shadows=shadows),
+                  noise_seed=5, frames=2, out_rgb=out, primitive=prim)
+        counts.append(ctx.ray_count())
+    ctx.check()
+    scene.close()
+    covered = int((sc["primitive"] == 0).sum())
+    assert 0 < counts[0] <= 2 * 2 * covered
+    assert counts[1] == counts[0]
+    assert counts[2] == 0
