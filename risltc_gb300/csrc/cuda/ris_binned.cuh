@@ -174,8 +174,10 @@ RL_DEV float clipped_integral(const mat43& t, const float4* record, uint32_t n, 
 // clips the polygon partially; the caller defers the item.
 template <class P, bool kChecked>
 RL_DEV bool binned_candidate(const float4* f, const float4* record, bool allow_clip, float& p_hat) {
-	// kChecked: normalise with normalize_checked and return false (the item
-	// is deferred) if any square root falls outside its range.
+	// kChecked: the branch-free forms (normalize_checked,
+	// integrate_edge_checked, sqrt_checked); false when any of them does not
+	// apply (a squared length outside the square root's range, an edge of 90
+	// degrees or more), and the caller takes the general forms.
 	bool ok = true;
 	const float4 head = __ldg(record), pl = __ldg(record + 1);
 	const uint32_t n = __float_as_uint(head.w);
