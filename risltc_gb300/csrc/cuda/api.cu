@@ -751,9 +751,12 @@ int reserve_candidates(risltc_ctx_t* ctx, size_t need) {
 	return RISLTC_OK;
 }
 
-size_t phat_region_floats(const risltc_ctx_t* ctx) {
+// One region: a p_hat slot per warp of the largest candidate grid, then 64
+// words whose first is the region's tile cursor.
+size_t phat_slot_floats(const risltc_ctx_t* ctx) {
 	return (size_t) ctx->sm_count * risltc::kCandidateBlocksPerSm * risltc::kBinnedWarps * risltc::kPHatSlot;
 }
+size_t phat_region_floats(const risltc_ctx_t* ctx) { return phat_slot_floats(ctx) + 64; }
 
 int reserve_phat(risltc_ctx_t* ctx, int regions) {
 	if (regions <= ctx->phat_regions) return RISLTC_OK;
@@ -807,6 +810,7 @@ risltc::RisParams ris_params(const risltc_ctx_t* ctx, const Scratch& sc, const r
 	r.frame_count = frame_count;
 	r.records = sc.records;
 	r.p_hat_scratch = sc.p_hat;
+	r.tile_cursor = sc.p_hat ? reinterpret_cast<uint32_t*>(sc.p_hat + phat_slot_floats(ctx)) : nullptr;
 	if (ray_queue) {
 		r.samples = sc.samples;
 		r.staged = sc.staged;
@@ -1147,6 +1151,7 @@ int shade_batch_fused(risltc_ctx_t* ctx, const risltc_batch_item_t* items, uint3
 		memset(&b, 0, sizeof(b));
 		b.count = gn;
 		b.p_hat_scratch = ctx->d_phat;
+		b.tile_cursor = reinterpret_cast<uint32_t*>(ctx->d_phat + phat_slot_floats(ctx));
 		b.ray_cursor = ctx->d_ray_count + 2 * queues;
 		uint32_t tiles = 0, pixels = 0, pfs = 0;
 		const size_t l_begin = l_off;

@@ -30,6 +30,7 @@ struct RisBatch {
 	uint32_t pf_begin[kBatchItems + 1];
 	// The candidate kernel's per-warp p_hat slots (for the launch's grid).
 	float* p_hat_scratch;
+	uint32_t* tile_cursor;  // the next warp tile over all items (zeroed before each launch)
 	// Fetch cursor of the batch's concatenated ray queue (zeroed by the scan
 	// kernel); the items' queue lengths are in their ray_count[0].
 	uint32_t* ray_cursor;
@@ -58,7 +59,7 @@ ris_candidates_batch_kernel(const __grid_constant__ RisBatch b) {
 	Tile& tile = reinterpret_cast<Tile*>(smem_raw)[threadIdx.x / 32];
 	float* const phat = b.p_hat_scratch + (size_t) (blockIdx.x * kBinnedWarps + threadIdx.x / 32) * kPHatSlot;
 	const uint32_t tiles = b.tile_begin[b.count];
-	for (uint32_t u = blockIdx.x * kBinnedWarps + threadIdx.x / 32; u < tiles; u += gridDim.x * kBinnedWarps) {
+	for (uint32_t u = next_warp_tile(b.tile_cursor); u < tiles; u = next_warp_tile(b.tile_cursor)) {
 		const uint32_t k = batch_item(b.tile_begin, b.count, u);
 		binned_tile<P, kPixels, kChunk>(b.item[k], tile, phat, u - b.tile_begin[k]);
 	}
@@ -72,6 +73,8 @@ cudaError_t launch_candidates_batch(const RisBatch& b, cudaStream_t stream, int 
 	const cudaError_t e = configure_candidate_kernel(ris_candidates_batch_kernel<P, kPixels, kChunk>,
 	                                                 binned_smem_bytes<P, kPixels, kChunk>(), configured, resident, device);
 	if (e != cudaSuccess) return e;
+	const cudaError_t z = cudaMemsetAsync(b.tile_cursor, 0, sizeof(uint32_t), stream);
+	if (z != cudaSuccess) return z;
 	const size_t blocks = ((size_t) b.tile_begin[b.count] + kBinnedWarps - 1) / kBinnedWarps;
 	const int grid = (int) std::max<size_t>(
 	    1, std::min<size_t>(blocks, (size_t) std::min(grid_cap, resident[device & 63].load())));

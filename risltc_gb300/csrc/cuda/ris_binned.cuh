@@ -54,6 +54,15 @@ constexpr int kPHatSlot = 4096;
 // one resident wave); the p_hat scratch has a slot per warp of such a grid.
 constexpr int kCandidateBlocksPerSm = 8;
 
+// The warp's next tile from the launch's cursor (lane 0 takes it, the warp
+// shares it): warps take tiles as they finish the previous one, so no warp
+// is left with a tail of tiles while the others idle.
+RL_DEV uint32_t next_warp_tile(uint32_t* cursor) {
+	uint32_t t = 0;
+	if (threadIdx.x % 32 == 0) t = atomicAdd(cursor, 1u);
+	return __shfl_sync(0xffffffffu, t, 0);
+}
+
 // Candidates per pixel per super-chunk (measured best: 32 in exact numerics,
 // 16 in fast numerics, where the smaller tile leaves more L1 for the lights).
 #ifndef RISLTC_BINNED_SUPER_EXACT
@@ -722,7 +731,7 @@ ris_candidates_binned_kernel(const __grid_constant__ RisParams pr) {
 	Tile& tile = reinterpret_cast<Tile*>(smem_raw)[threadIdx.x / 32];
 	float* const phat = pr.p_hat_scratch + (size_t) (blockIdx.x * kBinnedWarps + threadIdx.x / 32) * kPHatSlot;
 	const uint32_t tiles = (pr.width * pr.height + kPixels - 1) / kPixels;
-	for (uint32_t t = blockIdx.x * kBinnedWarps + threadIdx.x / 32; t < tiles; t += gridDim.x * kBinnedWarps)
+	for (uint32_t t = next_warp_tile(pr.tile_cursor); t < tiles; t = next_warp_tile(pr.tile_cursor))
 		binned_tile<P, kPixels, kChunk>(pr, tile, phat, t);
 }
 
@@ -776,6 +785,8 @@ cudaError_t launch_candidates_binned(const RisParams& p, cudaStream_t stream, in
 	const cudaError_t e = configure_candidate_kernel(ris_candidates_binned_kernel<P, kPixels, kChunk>,
 	                                                 binned_smem_bytes<P, kPixels, kChunk>(), configured, resident, device);
 	if (e != cudaSuccess) return e;
+	const cudaError_t z = cudaMemsetAsync(p.tile_cursor, 0, sizeof(uint32_t), stream);
+	if (z != cudaSuccess) return z;
 	ris_candidates_binned_kernel<P, kPixels, kChunk>
 	    <<<std::min(grid, resident[device & 63].load()), 32 * kBinnedWarps, binned_smem_bytes<P, kPixels, kChunk>(),
 	       stream>>>(p);

@@ -43,6 +43,7 @@ struct RisParams {
 	// floats per warp of the grid); null selects the one-thread-per-pixel
 	// candidate kernel.
 	float* p_hat_scratch;
+	uint32_t* tile_cursor;         // the binned candidate kernel's next warp tile (zeroed before each launch)
 	// Candidates drawn by a proposal ([frame][pixel][candidate]); null: each
 	// candidate is drawn uniformly from the pixel's noise as in the reference.
 	const ProposalCandidate* candidates;
