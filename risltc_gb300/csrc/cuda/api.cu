@@ -752,7 +752,7 @@ int reserve_candidates(risltc_ctx_t* ctx, size_t need) {
 }
 
 // One region: a p_hat slot per warp of the largest candidate grid, then 64
-// words whose first is the region's tile cursor.
+// words whose first two are the region's candidate-tile and sample cursors.
 size_t phat_slot_floats(const risltc_ctx_t* ctx) {
 	return (size_t) ctx->sm_count * risltc::kCandidateBlocksPerSm * risltc::kBinnedWarps * risltc::kPHatSlot;
 }
@@ -811,6 +811,7 @@ risltc::RisParams ris_params(const risltc_ctx_t* ctx, const Scratch& sc, const r
 	r.records = sc.records;
 	r.p_hat_scratch = sc.p_hat;
 	r.tile_cursor = sc.p_hat ? reinterpret_cast<uint32_t*>(sc.p_hat + phat_slot_floats(ctx)) : nullptr;
+	r.sample_cursor = r.tile_cursor ? r.tile_cursor + 1 : nullptr;
 	if (ray_queue) {
 		r.samples = sc.samples;
 		r.staged = sc.staged;

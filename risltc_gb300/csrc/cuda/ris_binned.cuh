@@ -54,15 +54,6 @@ constexpr int kPHatSlot = 4096;
 // one resident wave); the p_hat scratch has a slot per warp of such a grid.
 constexpr int kCandidateBlocksPerSm = 8;
 
-// The warp's next tile from the launch's cursor (lane 0 takes it, the warp
-// shares it): warps take tiles as they finish the previous one, so no warp
-// is left with a tail of tiles while the others idle.
-RL_DEV uint32_t next_warp_tile(uint32_t* cursor) {
-	uint32_t t = 0;
-	if (threadIdx.x % 32 == 0) t = atomicAdd(cursor, 1u);
-	return __shfl_sync(0xffffffffu, t, 0);
-}
-
 // Candidates per pixel per super-chunk (measured best: 32 in exact numerics,
 // 16 in fast numerics, where the smaller tile leaves more L1 for the lights).
 #ifndef RISLTC_BINNED_SUPER_EXACT

@@ -24,6 +24,15 @@ struct ReservoirRecord {
 	uint32_t seed;  // noise state after the candidate loop
 };
 
+// The warp's next tile from the launch's cursor (lane 0 takes it, the warp
+// shares it): warps take tiles as they finish the previous one, so no warp
+// is left with a tail of tiles while the others idle.
+RL_DEV uint32_t next_warp_tile(uint32_t* cursor) {
+	uint32_t t = 0;
+	if (threadIdx.x % 32 == 0) t = atomicAdd(cursor, 1u);
+	return __shfl_sync(0xffffffffu, t, 0);
+}
+
 struct RisParams {
 	SceneView scene;
 	const float* gbuffer;
@@ -44,6 +53,7 @@ struct RisParams {
 	// candidate kernel.
 	float* p_hat_scratch;
 	uint32_t* tile_cursor;         // the binned candidate kernel's next warp tile (zeroed before each launch)
+	uint32_t* sample_cursor;       // the sample kernel's next 32 pixels (zeroed before each launch)
 	// Candidates drawn by a proposal ([frame][pixel][candidate]); null: each
 	// candidate is drawn uniformly from the pixel's noise as in the reference.
 	const ProposalCandidate* candidates;
@@ -350,6 +360,7 @@ inline cudaError_t launch_ris(const RisParams& p, cudaStream_t stream, int grid,
 	if (events) cudaEventRecord(events[1], stream);
 	if (p.samples) {
 		e = cudaMemsetAsync(p.light_rays, 0, sizeof(uint32_t) * p.scene.light_count * kLightCounterStride, stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(p.sample_cursor, 0, sizeof(uint32_t), stream);
 		if (e == cudaSuccess) e = launch_ris_sample(p, stream, grid);
 		if (e != cudaSuccess) return e;
 		if (events) cudaEventRecord(events[2], stream);

@@ -241,12 +241,14 @@ template <class P> RL_DEV void sample_pixel(const RisParams& pr, uint32_t i, Psa
 	}
 }
 
+// Each warp takes 32 consecutive pixels at a time from the launch's cursor.
 template <class P>
 __global__ void __launch_bounds__(kSampleThreads, RISLTC_SAMPLE_MIN_BLOCKS) ris_sample_kernel(const __grid_constant__ RisParams pr) {
 	__shared__ PsaPolygon poly[kSampleThreads];
 	const uint32_t np = pr.width * pr.height;
-	for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += gridDim.x * blockDim.x)
-		sample_pixel<P>(pr, base + threadIdx.x, poly[threadIdx.x]);
+	const uint32_t chunks = (np + 31) / 32;
+	for (uint32_t c = next_warp_tile(pr.sample_cursor); c < chunks; c = next_warp_tile(pr.sample_cursor))
+		sample_pixel<P>(pr, c * 32 + threadIdx.x % 32, poly[threadIdx.x]);
 }
 
 // Exclusive prefix sum of the per-light ray counts, in place (each becomes
