@@ -38,3 +38,18 @@ def test_default_workload_is_the_headline_configuration():
     assert bench.is_headline(a) and bench.metric_name(a) == bench.HEADLINE_METRIC
     b = bench.parse(["--workload", "throughput"])
     assert (b.lights, b.triangles, b.clusters) == (1024, 200_000, 0)
+
+
+def test_reference_arm_under_two_ranks_prints_once():
+    """Launched as the multi-GPU bench is (torchrun, two ranks), the reference
+    arm runs on rank 0 alone: one JSON line in all, and every rank exits 0."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", "29531", os.path.join(REPO, "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--width", "64", "--height", "36", "--lights", "16",
+           "--clusters", "4", "--triangles", "200", "--steps", "3", "--warmup", "3", "--cpu-seconds", "0.1"]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [line for line in out.stdout.splitlines() if line.strip().startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
