@@ -733,8 +733,8 @@ template <class P, int kPixels, int kChunk> constexpr size_t binned_smem_bytes()
 // First launch of a candidate kernel on a device: raises its shared-memory
 // limit (above the 48 KB available without opting in) and stores in
 // resident[device] the blocks that fit on the device at once (resident
-// blocks per SM times the SM count), the kernel's persistent grid: its warps
-// stride over the tiles in one wave, with no partial last wave.  Done once
+// blocks per SM times the SM count), the kernel's persistent grid: one wave
+// whose warps take tiles from the launch's cursor until none is left.  Done once
 // per device, so that later launches, including those captured into a CUDA
 // graph, make no other runtime call.
 template <class Kernel>
