@@ -53,3 +53,45 @@ def test_reference_arm_under_two_ranks_prints_once():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_roofline_arithmetic_of_the_bench_line():
+    """The bench line's per-kernel table and roofline from given CUDA-event
+    times and op counts: achieved = FLOP per pixel-sample x pixel-samples per
+    launch / launch time, frac = achieved / peak, the dominant kernel the
+    slowest, DRAM traffic scaled from the captured launch's pixel-samples."""
+    sys.path.insert(0, REPO)
+    import bench
+    calls = 4
+    prof = {"calls": calls, "candidates": 4 * 14.0, "shade": 4 * 3.5, "ray_sort": 4 * 0.5, "shadow_trace": 4 * 5.0,
+            "resolve": 4 * 0.25}
+    info = {"flops_per_sample": 26000.0, "candidate_flops_per_sample": 23000.0, "shade_flops_per_sample": 3000.0,
+            "trace_flops_per_sample": 1500.0, "trace_bytes_per_sample": 2800.0}
+    samples = 8_294_400
+    peak = 80.0
+    k = bench.kernel_table(prof, samples, info, peak, {})
+    cand = k["ris_candidates_binned_kernel"]
+    assert cand["ms_per_launch"] == 14.0
+    want = 23000.0 * samples / 14e-3 / 1e12
+    assert abs(cand["achieved_tflops"] - want) <= 1e-9 * want and abs(cand["frac"] - want / peak) <= 1e-12
+    tr = k["shadow_trace_kernel"]
+    assert abs(tr["node_triangle_gbs"] - 2800.0 * samples / 5e-3 / 1e9) <= 1e-6
+    assert k["ris_resolve_kernel"]["achieved_tflops"] == 0.0
+    bench.attach_dram(k, "many_lights_1080p", samples, {"hbm_gbs": 7000.0})
+    with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+        t = json.load(f)["many_lights_1080p"]["ris_candidates_binned_kernel"]
+    dram = t["dram_bytes"] * samples / t["pixel_samples"]
+    assert abs(cand["dram_bytes_per_launch"] - dram) <= 1e-6 * dram
+    assert abs(cand["dram_frac_of_hbm"] - dram / 14e-3 / 1e9 / 7000.0) <= 1e-12
+    ms_step = 23.25
+    r = bench.roofline_of(k, peak, info["flops_per_sample"], samples, ms_step, 152, 2070.0, "many_lights_1080p")
+    assert r["kernel"] == "ris_candidates_binned_kernel" and r["unit"] == "TFLOP/s" and r["peak"] == peak
+    assert r["achieved"] == cand["achieved_tflops"] and r["frac"] == cand["frac"]
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) <= 1e-12
+    assert abs(r["traffic"] - dram) <= 1e-6 * dram
+    assert abs(r["whole_step_frac"] - 26000.0 * samples / (ms_step / 1e3) / 1e12 / peak) <= 1e-12
+    a = bench.parse([])
+    rates = bench.rates_of(a, {"value": 0.35, "ms_per_step": ms_step, "rays_per_step": 16_000_000}, k)
+    assert abs(rates["gcandidates_per_s"] - 0.35 * 32) <= 1e-12
+    assert abs(rates["grays_per_s_trace_kernel"] - 16e6 / 5e-3 / 1e9) <= 1e-9
+    assert bench.rates_of(a, {"value": 0.35, "ms_per_step": ms_step}, k)["grays_per_s_step"] is None
