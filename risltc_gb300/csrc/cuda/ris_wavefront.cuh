@@ -255,7 +255,6 @@ __global__ void __launch_bounds__(kSampleThreads, RISLTC_SAMPLE_MIN_BLOCKS) ris_
 // its bucket's first queue position); the total goes to ray_count[0] and the
 // trace kernel's fetch cursor ray_count[1] is reset.  One block of 1024
 // threads.
-// The scan by one block of 1024 threads.
 RL_DEV void light_bucket_scan(uint32_t* light_rays, uint32_t light_count, uint32_t* ray_count) {
 	__shared__ uint32_t warp_offset[32];
 	__shared__ uint32_t chunk_total;
