@@ -164,7 +164,8 @@ EXTERN_C uint32_t risltc_wang_random_number(uint32_t seed);
    unwritten).  Calls update_polygonal_light() on each light.  data must hold
    count * (12 + 4 * max_vertex_count) floats. */
 EXTERN_C int risltc_write_lights(float* data, polygonal_light_t* lights, uint32_t count, uint32_t max_vertex_count);
-/* get_max_polygonal_light_vertex_count, src/main.c:183-189 */
+/* get_max_polygonal_light_vertex_count, src/main.c:183-189 (at least 3; no
+   lights, or a null array, gives 3) */
 EXTERN_C uint32_t risltc_max_light_vertex_count(const polygonal_light_t* lights, uint32_t count);
 
 /* LTC table in FP32 (the reference keeps two UNORM16 texture arrays,
@@ -320,7 +321,8 @@ typedef struct risltc_settings_s {
 	risltc_tile_t tile;         /* candidate kernel tile shape (default configuration only) */
 } risltc_settings_t;
 
-/* specify_default_render_settings, src/main.c:220-236 (M = 32, shadows on) */
+/* specify_default_render_settings, src/main.c:220-236 (M = 32, shadows on;
+   a null pointer is ignored) */
 EXTERN_C void risltc_default_settings(risltc_settings_t* settings);
 
 /* G-buffer: 17 planes of width*height floats in device memory (the fields

@@ -123,7 +123,7 @@ void set_noise_constants(uint32_t resolution_mask[2], uint32_t* texture_index_ma
 
 uint32_t risltc_max_light_vertex_count(const polygonal_light_t* lights, uint32_t count) {
 	uint32_t m = 3;
-	for (uint32_t i = 0; i != count; ++i)
+	for (uint32_t i = 0; lights && i != count; ++i)
 		if (lights[i].vertex_count > m) m = lights[i].vertex_count;
 	return m;
 }
@@ -156,6 +156,7 @@ int risltc_write_lights(float* data, polygonal_light_t* lights, uint32_t count, 
 }
 
 void risltc_default_settings(risltc_settings_t* s) {
+	if (!s) return;
 	memset(s, 0, sizeof(*s));
 	s->polygon_sampling_technique = sample_polygon_ltc_cp;
 	s->light_sampling = light_reservoir;

@@ -29,6 +29,46 @@ def test_library_exports_every_declared_function(lib):
         assert hasattr(lib, n), n
 
 
+NULL_ARGUMENT_CHECK = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+from risltc_gb300 import _native as n
+lib = n.load(build_if_missing=False)
+# The reference's own light and noise functions dereference their arguments
+# as the reference does; every function of this library checks them.
+reference_api = {"set_polygonal_light_vertex_count", "update_polygonal_light", "duplicate_polygonal_light",
+                 "destroy_polygonal_light", "set_noise_constants"}
+checked = 0
+for name, (res, args) in sorted(n.SIGNATURES.items()):
+    if name in reference_api:
+        continue
+    for fill in (0, 1):
+        vals = [fill if a in (ctypes.c_uint32, ctypes.c_int, ctypes.c_uint64) else float(fill)
+                if a is ctypes.c_float else None for a in args]
+        r = getattr(lib, name)(*vals)
+        if res is ctypes.c_int:
+            assert r == 1, (name, fill, r)  # RISLTC_ERROR_INVALID_ARGUMENT
+            checked += 1
+assert lib.risltc_max_light_vertex_count(None, 5) == 3
+print(checked)
+"""
+
+
+def test_entry_points_reject_null_handles_and_arrays(lib):
+    """Every status-returning entry point of this library answers null
+    handles and arrays (with zero and non-zero counts) with
+    RISLTC_ERROR_INVALID_ARGUMENT before it touches a device, and the
+    functions without a status (destroy, default settings) accept null.
+    Run in a child process, so that a null dereference fails the test
+    instead of ending the test run."""
+    out = subprocess.run([os.sys.executable, "-c", NULL_ARGUMENT_CHECK, REPO], capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    from risltc_gb300 import _native
+    statuses = [k for k, (res, _) in _native.SIGNATURES.items() if res is ctypes.c_int and k.startswith("risltc_")]
+    assert len(statuses) >= 35 and int(out.stdout.strip()) == 2 * len(statuses)
+
+
 def test_math_kernels_against_libm(tmp_path):
     src = tmp_path / "m.c"
     src.write_text('#include "risltc_math.h"\n'
