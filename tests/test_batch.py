@@ -145,3 +145,46 @@ def test_whole_batch_launches_equal_single_calls(gpu, tile):
     for sc in scenes:
         sc.close()
     ctx.close()
+
+
+def test_single_call_graph_replay_equals_direct_call(gpu):
+    """One risltc_shade call of the default configuration (shadow rays
+    through the ray queue, two frames, FP64 sums and reservoirs), captured
+    into a CUDA graph after a first call has sized the scratch: every replay
+    equals the same call made directly, bit for bit."""
+    import torch
+    import risltc_gb300 as rl
+    hs = rl.scenes.plane_of_quads(160, 96, 200, seed=31, triangles=3000)
+    stream = torch.cuda.Stream()
+    ctx = rl.Context(0, stream=stream.cuda_stream)
+    sc = rl.Scene.from_host_scene(ctx, hs)
+    s = rl.settings(candidates=16)
+
+    def buffers():
+        return (torch.full((hs.pixels, 3), -1.0, dtype=torch.float32, device="cuda"),
+                torch.zeros((hs.pixels, 3), dtype=torch.float64, device="cuda"),
+                torch.zeros((hs.pixels, 4), dtype=torch.int32, device="cuda"))
+    with torch.cuda.stream(stream):
+        g = torch.from_numpy(hs.gbuffer).cuda()
+        want = buffers()
+        assert rl.shade(ctx, sc, g, hs.width, hs.height, s, noise_seed=9, frames=2, out_rgb=want[0], accum=want[1],
+                        reservoirs=want[2]) == 11
+        got = buffers()
+    torch.cuda.synchronize()
+    ctx.check()
+    assert ctx.ray_count() > 0
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        rl.shade(ctx, sc, g, hs.width, hs.height, s, noise_seed=9, frames=2, out_rgb=got[0], accum=got[1],
+                 reservoirs=got[2])
+    for _ in range(2):
+        got[0].fill_(-1.0)
+        got[1].zero_()
+        got[2].zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+        ctx.check()
+        for a, b in zip(got, want):
+            assert torch.equal(a, b)
+    sc.close()
+    ctx.close()
