@@ -480,9 +480,13 @@ EXTERN_C void risltc_scene_destroy(risltc_scene_t* scene);
  * frame_count frames per call: 16 bytes per pixel and frame of reservoir
  * records between the candidate and shading kernels (used by the default
  * configuration: LTC-CP, light_reservoir, one light sample).  risltc_shade
- * grows the scratch itself when needed (a device allocation); calling this
- * first keeps later risltc_shade calls free of allocations, e.g. for stream
- * capture into a CUDA graph. */
+ * grows the scratch itself when needed (device allocations: these records,
+ * the candidate kernel's p_hat slots and, with shadow rays, the ray queue,
+ * whose per-light counters depend on the scene) and configures each kernel
+ * on its first launch.  After one call, later calls that need no more
+ * scratch (no more pixels, frames, lights, candidates or clusters) make no
+ * allocation and no configuration call; a default-configuration call made
+ * after one such call can be captured into a CUDA graph. */
 EXTERN_C int risltc_ctx_reserve(risltc_ctx_t* ctx, uint32_t width, uint32_t height, uint32_t frame_count);
 
 /* Shades frame_count consecutive frames of the G-buffer (device pointers).
